@@ -1,0 +1,146 @@
+/*
+ * sfmm.h -- C ABI of solidfmm-gb300: GB300 (sm_103a) translation operators
+ * M2M, M2L and L2L on solid-harmonic expansions.
+ *
+ * This is the only CUDA-facing surface.  The C++ drop-in headers under
+ * include/solidfmm/ (solid, harmonics, handles, translations,
+ * multithreaded_translator) are implemented on top of it.
+ *
+ * Expansion layout (identical to the reference's solid<real>,
+ * solidfmm/solid.hpp:59-60): an expansion of order P holds P(P+1) reals; for
+ * degree n < P the n+1 real parts re(n,0..n) start at n(n+1) and the n+1
+ * imaginary parts im(n,0..n) start at (n+1)^2.  Batches address expansions in
+ * a uniform-stride array: expansion j starts at base + j*stride reals.
+ *
+ * Semantics of every translation call (solidfmm/translations.hpp:94-170):
+ *   target += T(source, shift),  shift = new centre - old centre,
+ * with per-translation source order P_in and target order P_out, both at most
+ * the context's order.  M2M and L2L with a zero shift add the first
+ * min(P_in,P_out) degrees directly (solidfmm/translations.cpp:540-547).
+ *
+ * Errors never cross the ABI as exceptions: every function returns an
+ * sfmm_status; sfmm_last_error() describes the last failure on a context.
+ */
+#ifndef SFMM_H
+#define SFMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SFMM_OK = 0,
+    SFMM_INVALID_ARG = 1,   /* std::logic_error in the reference (e.g. P == 0, incompatible buffer) */
+    SFMM_ORDER_RANGE = 2,   /* std::out_of_range: an order exceeds the operator order */
+    SFMM_OVERFLOW = 3,      /* std::overflow_error: order too large for the floating-point type */
+    SFMM_DIM_MISMATCH = 4,  /* std::logic_error: source and target dimensions differ */
+    SFMM_OOM = 5,           /* std::bad_alloc */
+    SFMM_CUDA_ERROR = 6,    /* CUDA runtime failure (no device, launch failure, ...) */
+    SFMM_UNSUPPORTED = 7    /* precision mode not available for this data type */
+} sfmm_status;
+
+typedef enum { SFMM_F32 = 0, SFMM_F64 = 1 } sfmm_dtype;
+typedef enum { SFMM_M2M = 0, SFMM_M2L = 1, SFMM_L2L = 2 } sfmm_op;
+
+/* Arithmetic of the translation kernels.
+ * PLAIN: the storage type's own arithmetic (FP64 for SFMM_F64, FP32 for SFMM_F32).
+ * SPLIT: double-FP32 (float-float) arithmetic on the FP32 pipes for every
+ *        swap, rotation and z-translation; FP64 geometry and FP64 final
+ *        accumulation into the targets.  SFMM_F64 contexts only. */
+typedef enum { SFMM_PLAIN = 0, SFMM_SPLIT = 1 } sfmm_precision;
+
+/* flags for the batch calls */
+enum {
+    SFMM_TARGETS_UNIQUE = 0,   /* no two translations of the batch share a target */
+    SFMM_TARGETS_REPEAT = 1    /* targets may repeat: accumulate with atomics */
+};
+
+typedef struct sfmm_context sfmm_context;
+
+/* Operator context of order P (the reference's operator_data<real>(P),
+ * solidfmm/operator_data.cpp:151-244): builds the rotation/swap/z-translation
+ * tables in FP64 on the host and uploads them to `device`.
+ * P == 0 -> SFMM_INVALID_ARG; P > 18 (F32) or P > 86 (F64) -> SFMM_OVERFLOW
+ * (the reference's limits, operator_data.cpp:37-45,157-164). */
+int sfmm_create(sfmm_context **ctx, int dtype, size_t P, int device);
+void sfmm_destroy(sfmm_context *ctx);
+size_t sfmm_order(const sfmm_context *ctx);
+int sfmm_data_type(const sfmm_context *ctx);
+const char *sfmm_last_error(const sfmm_context *ctx);
+const char *sfmm_status_string(int status);
+
+/* All kernels of the context are launched on this CUDA stream (cudaStream_t
+ * passed as void*; NULL = the legacy default stream). */
+int sfmm_set_stream(sfmm_context *ctx, void *stream);
+
+/* Device-resident batch (all pointers are device pointers; replaces the
+ * lane queues of solidfmm/translations.cpp:474-630 and the worker loop of
+ * solidfmm/multithreaded_translator.cpp:261-330).  Translation i:
+ *   dst[dst_index[i]] += T_op(src[src_index[i]], shift[3i..3i+2])
+ * with orders p_in[i], p_out[i] <= order_bound (0 = the context order).
+ * src_index/dst_index NULL mean i; src_count/dst_count are the numbers of
+ * expansions addressable through src/dst.  `order` (may be NULL) is a
+ * permutation giving the processing order (see sfmm_bucket_by_order).
+ * Shifts are FP64 for both data types.  Asynchronous on the context's stream.
+ * Entries with an index or order out of range are skipped and flagged in the
+ * context's device status word (sfmm_device_status); they never touch memory
+ * out of bounds.  Targets must not alias sources. */
+int sfmm_translate_device(sfmm_context *ctx, int op, int precision, size_t n,
+                          const void *src, size_t src_stride, size_t src_count, const uint32_t *src_index,
+                          void *dst, size_t dst_stride, size_t dst_count, const uint32_t *dst_index,
+                          const uint32_t *p_in, const uint32_t *p_out, const double *shift,
+                          const uint32_t *order, int flags, size_t order_bound);
+
+/* Synchronise the context's stream and return (and clear) its device status
+ * word: 0 = every translation since the last call was well formed, bit 0 =
+ * some entry had an out-of-range index or order and was skipped. */
+int sfmm_device_status(sfmm_context *ctx, int *flags);
+
+/* Contiguous host batch, the bulk form of the classic call: src/dst are HOST
+ * arrays of src_count/dst_count expansions with the given strides (pinned
+ * memory gives full copy bandwidth), orders/indices/shifts are host arrays as
+ * in sfmm_translate_device.  Copies in, translates, copies the updated
+ * targets back and synchronises before returning.  Batches without index
+ * arrays are pipelined in chunks over three streams so that host-to-device
+ * copies, kernels and device-to-host copies overlap. */
+int sfmm_translate_host_packed(sfmm_context *ctx, int op, int precision, size_t n,
+                               const void *src, size_t src_stride, size_t src_count, const uint32_t *src_index,
+                               void *dst, size_t dst_stride, size_t dst_count, const uint32_t *dst_index,
+                               const uint32_t *p_in, const uint32_t *p_out, const double *shift, int flags);
+
+/* Host drop-in batch: the classic solidfmm::m2l/m2m/l2l(op, buf, howmany,
+ * M**, L**, x, y, z) call (solidfmm/translations.hpp:103-109).  src[i] and
+ * dst[i] point at host expansions (in the solid layout, dim components of
+ * P(P+1) reals each); x/y/z are arrays of the context's real type.  Orders
+ * are checked first (strong guarantee: on error nothing is modified); the
+ * call gathers the expansions to the GPU, runs the batch, and scatter-adds
+ * the results into the host targets before returning. */
+int sfmm_translate_host(sfmm_context *ctx, int op, int precision, size_t n,
+                        const void *const *src, const size_t *p_in,
+                        void *const *dst, const size_t *p_out, size_t dim,
+                        const void *x, const void *y, const void *z);
+
+/* Bucket a device batch by (p_in, p_out): writes a permutation of 0..n-1 into
+ * `order` (device, n entries) so that translations of equal order pairs are
+ * contiguous.  Uses ctx scratch; asynchronous. */
+int sfmm_bucket_by_order(sfmm_context *ctx, size_t n, const uint32_t *p_in, const uint32_t *p_out,
+                         uint32_t *order);
+
+/* P2M / P2L on the device (the reference's fmadd(q, harmonics::R/S(P, x-c), E),
+ * solid.cpp:70-104 with harmonics.cpp:32-80,177-224): for expansion j,
+ *   out[j] += sum_{k<nq} charge[j*nq+k] * R(pos[j*nq+k] - centre[j])   (kind 0)
+ *   out[j] += sum_{k<nq} charge[j*nq+k] * S(pos[j*nq+k] - centre[j])   (kind 1)
+ * FP64 arithmetic; out has the context's data type and order P. */
+int sfmm_p2x_device(sfmm_context *ctx, int kind, size_t nexp, size_t nq, const double *charge,
+                    const double *pos, const double *centre, void *out, size_t out_stride);
+
+/* Number of kernel launches issued by this context since creation. */
+uint64_t sfmm_launch_count(const sfmm_context *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

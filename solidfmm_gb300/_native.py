@@ -1,0 +1,157 @@
+"""ctypes binding of the C ABI (include/sfmm.h) in libsfmm_gb300.so.
+
+The library is the product: there is no Python or CPU implementation of the
+translations behind this module.  Loading fails loudly if the library has not
+been built (python -m solidfmm_gb300.build).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+F32, F64 = 0, 1
+M2M, M2L, L2L = 0, 1, 2
+PLAIN, SPLIT = 0, 1
+TARGETS_UNIQUE, TARGETS_REPEAT = 0, 1
+OPS = {"m2m": M2M, "m2l": M2L, "l2l": L2L}
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "ORDER_RANGE", 3: "OVERFLOW", 4: "DIM_MISMATCH", 5: "OOM",
+          6: "CUDA_ERROR", 7: "UNSUPPORTED"}
+
+EXPORTS = [
+    "sfmm_create", "sfmm_destroy", "sfmm_order", "sfmm_data_type", "sfmm_last_error", "sfmm_status_string",
+    "sfmm_set_stream", "sfmm_translate_device", "sfmm_device_status", "sfmm_translate_host_packed",
+    "sfmm_translate_host", "sfmm_bucket_by_order", "sfmm_p2x_device", "sfmm_launch_count",
+]
+
+
+class SfmmError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load():
+    """Load libsfmm_gb300.so (must have been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"solidfmm_gb300 native library missing: {path} (run python -m solidfmm_gb300.build)")
+    L = C.CDLL(path)
+    vp, sz, u32p, dp = C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p
+    L.sfmm_create.argtypes = [C.POINTER(vp), C.c_int, sz, C.c_int]
+    L.sfmm_destroy.argtypes = [vp]
+    L.sfmm_destroy.restype = None
+    L.sfmm_order.argtypes = [vp]
+    L.sfmm_order.restype = sz
+    L.sfmm_data_type.argtypes = [vp]
+    L.sfmm_last_error.argtypes = [vp]
+    L.sfmm_last_error.restype = C.c_char_p
+    L.sfmm_status_string.argtypes = [C.c_int]
+    L.sfmm_status_string.restype = C.c_char_p
+    L.sfmm_set_stream.argtypes = [vp, vp]
+    L.sfmm_translate_device.argtypes = [vp, C.c_int, C.c_int, sz, vp, sz, sz, u32p, vp, sz, sz, u32p, u32p, u32p,
+                                        dp, u32p, C.c_int, sz]
+    L.sfmm_device_status.argtypes = [vp, C.POINTER(C.c_int)]
+    L.sfmm_translate_host_packed.argtypes = [vp, C.c_int, C.c_int, sz, vp, sz, sz, u32p, vp, sz, sz, u32p, u32p,
+                                             u32p, dp, C.c_int]
+    L.sfmm_translate_host.argtypes = [vp, C.c_int, C.c_int, sz, vp, vp, vp, vp, sz, vp, vp, vp]
+    L.sfmm_bucket_by_order.argtypes = [vp, sz, u32p, u32p, u32p]
+    L.sfmm_p2x_device.argtypes = [vp, C.c_int, sz, sz, dp, dp, dp, vp, sz]
+    L.sfmm_launch_count.argtypes = [vp]
+    L.sfmm_launch_count.restype = C.c_uint64
+    _lib = L
+    return L
+
+
+def _ptr(x):
+    """device/host address of a torch tensor or numpy array (None -> NULL)."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+class Context:
+    """An operator context (the reference's operator_data / operator_handle)."""
+
+    def __init__(self, P: int, dtype: str = "f64", device: int = 0):
+        L = load()
+        self.dtype = F64 if dtype in ("f64", "double", np.float64) else F32
+        h = C.c_void_p()
+        rc = L.sfmm_create(C.byref(h), self.dtype, P, device)
+        if rc:
+            raise SfmmError(rc, L.sfmm_status_string(rc).decode())
+        self.h = h
+        self.P = P
+        self.L = L
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sfmm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise SfmmError(rc, self.L.sfmm_last_error(self.h).decode())
+
+    @property
+    def launches(self) -> int:
+        return self.L.sfmm_launch_count(self.h)
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self.L.sfmm_set_stream(self.h, stream_ptr))
+
+    def translate_device(self, op, precision, n, src, src_stride, src_count, dst, dst_stride, dst_count, p_in, p_out,
+                         shift, src_index=None, dst_index=None, order=None, repeat=False, order_bound=0):
+        op = OPS.get(op, op)
+        self._check(self.L.sfmm_translate_device(
+            self.h, op, precision, n, _ptr(src), src_stride, src_count, _ptr(src_index), _ptr(dst), dst_stride,
+            dst_count, _ptr(dst_index), _ptr(p_in), _ptr(p_out), _ptr(shift), _ptr(order),
+            TARGETS_REPEAT if repeat else TARGETS_UNIQUE, order_bound))
+
+    def device_status(self) -> int:
+        v = C.c_int(0)
+        self._check(self.L.sfmm_device_status(self.h, C.byref(v)))
+        return v.value
+
+    def translate_host_packed(self, op, precision, src, dst, p_in, p_out, shift, src_index=None, dst_index=None,
+                              repeat=False):
+        op = OPS.get(op, op)
+        n = len(p_in)
+        p_in = np.ascontiguousarray(p_in, np.uint32)
+        p_out = np.ascontiguousarray(p_out, np.uint32)
+        shift = np.ascontiguousarray(shift, np.float64)
+        si = None if src_index is None else np.ascontiguousarray(src_index, np.uint32)
+        ti = None if dst_index is None else np.ascontiguousarray(dst_index, np.uint32)
+        self._check(self.L.sfmm_translate_host_packed(
+            self.h, op, precision, n, _ptr(src), src.shape[-1], src.shape[0], _ptr(si), _ptr(dst), dst.shape[-1],
+            dst.shape[0], _ptr(ti), _ptr(p_in), _ptr(p_out), _ptr(shift),
+            TARGETS_REPEAT if repeat else TARGETS_UNIQUE))
+
+    def bucket(self, n, p_in, p_out, order):
+        self._check(self.L.sfmm_bucket_by_order(self.h, n, _ptr(p_in), _ptr(p_out), _ptr(order)))
+
+    def p2x(self, kind, nexp, nq, charge, pos, centre, out, out_stride):
+        self._check(self.L.sfmm_p2x_device(self.h, kind, nexp, nq, _ptr(charge), _ptr(pos), _ptr(centre),
+                                           _ptr(out), out_stride))

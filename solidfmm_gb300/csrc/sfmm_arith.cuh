@@ -1,0 +1,153 @@
+// Arithmetic policies for the translation kernels.
+//
+//   double : plain FP64 (DFMA pipe)
+//   float  : plain FP32
+//   ff     : double-FP32 ("float-float", hi + lo) on the FP32 pipe.  Products
+//            are split exactly with an FMA (Dekker/Ogita-Rump-Oishi TwoProduct),
+//            sums use Knuth's TwoSum; accumulations keep an unnormalised low
+//            word and renormalise once at the end (Fast2Sum).  Every
+//            intermediate carries ~44+ bits, which keeps the relative error of a
+//            whole translation near 1e-13 although each operation runs on FP32.
+//            __fmul_rn/__fadd_rn stop the compiler from contracting the
+//            error-free transformations into FMAs.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace sfmm {
+
+struct ff {
+    float hi, lo;
+};
+
+template <class A>
+struct arith;
+
+template <>
+struct arith<double> {
+    using T = double;
+    using Stor = double;  // element type of the shared-memory buffer
+    using Acc = double;
+    static __device__ __forceinline__ T zero() { return 0.0; }
+    static __device__ __forceinline__ T from_d(double x) { return x; }
+    static __device__ __forceinline__ double to_d(T x) { return x; }
+    static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+    static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+    static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
+    static __device__ __forceinline__ T neg(T a) { return -a; }
+    static __device__ __forceinline__ Acc acc0() { return 0.0; }
+    static __device__ __forceinline__ void mac(Acc &acc, T w, T x) { acc = fma(w, x, acc); }
+    static __device__ __forceinline__ T fin(Acc a) { return a; }
+    static __device__ __forceinline__ T ld(const Stor *p) { return *p; }
+    static __device__ __forceinline__ void st(Stor *p, T v) { *p = v; }
+    static __device__ __forceinline__ T ldt(const T *p) { return __ldg(p); }
+};
+
+template <>
+struct arith<float> {
+    using T = float;
+    using Stor = float;
+    using Acc = float;
+    static __device__ __forceinline__ T zero() { return 0.f; }
+    static __device__ __forceinline__ T from_d(double x) { return (float)x; }
+    static __device__ __forceinline__ double to_d(T x) { return (double)x; }
+    static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+    static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+    static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
+    static __device__ __forceinline__ T neg(T a) { return -a; }
+    static __device__ __forceinline__ Acc acc0() { return 0.f; }
+    static __device__ __forceinline__ void mac(Acc &acc, T w, T x) { acc = fmaf(w, x, acc); }
+    static __device__ __forceinline__ T fin(Acc a) { return a; }
+    static __device__ __forceinline__ T ld(const Stor *p) { return *p; }
+    static __device__ __forceinline__ void st(Stor *p, T v) { *p = v; }
+    static __device__ __forceinline__ T ldt(const T *p) { return __ldg(p); }
+};
+
+// Fast2Sum: |a| >= |b| assumed (or a == 0)
+__device__ __forceinline__ ff ff_norm(float a, float b)
+{
+    float s = __fadd_rn(a, b);
+    float e = __fsub_rn(b, __fsub_rn(s, a));
+    return ff{s, e};
+}
+
+__device__ __forceinline__ ff ff_from_d(double x)
+{
+    float h = __double2float_rn(x);
+    float l = __double2float_rn(x - (double)h);
+    return ff{h, l};
+}
+
+__device__ __forceinline__ double ff_to_d(ff a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ ff ff_add(ff a, ff b)
+{
+    float s = __fadd_rn(a.hi, b.hi);
+    float v = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    return ff_norm(s, e);
+}
+
+__device__ __forceinline__ ff ff_mul(ff a, ff b)
+{
+    float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return ff_norm(p, e);
+}
+
+// unnormalised accumulator: value = hi + lo, lo collects every rounding error
+struct ffacc {
+    float hi, lo;
+};
+
+template <>
+struct arith<ff> {
+    using T = ff;
+    using Stor = float2;
+    using Acc = ffacc;
+    static __device__ __forceinline__ T zero() { return ff{0.f, 0.f}; }
+    static __device__ __forceinline__ T from_d(double x) { return ff_from_d(x); }
+    static __device__ __forceinline__ double to_d(T x) { return ff_to_d(x); }
+    static __device__ __forceinline__ T mul(T a, T b) { return ff_mul(a, b); }
+    static __device__ __forceinline__ T add(T a, T b) { return ff_add(a, b); }
+    static __device__ __forceinline__ T sub(T a, T b) { return ff_add(a, ff{-b.hi, -b.lo}); }
+    static __device__ __forceinline__ T neg(T a) { return ff{-a.hi, -a.lo}; }
+    static __device__ __forceinline__ Acc acc0() { return ffacc{0.f, 0.f}; }
+    // acc += w * x, 11 FP32 operations
+    static __device__ __forceinline__ void mac(Acc &acc, T w, T x)
+    {
+        float p = __fmul_rn(w.hi, x.hi);
+        float e = __fmaf_rn(w.hi, x.hi, -p);
+        e = __fmaf_rn(w.hi, x.lo, e);
+        e = __fmaf_rn(w.lo, x.hi, e);
+        float s = __fadd_rn(acc.hi, p);
+        float v = __fsub_rn(s, acc.hi);
+        float t = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, v)), __fsub_rn(p, v));
+        acc.lo = __fadd_rn(acc.lo, __fadd_rn(t, e));
+        acc.hi = s;
+    }
+    static __device__ __forceinline__ T fin(Acc a)
+    {
+        // two-sum renormalisation (lo may exceed hi after cancellation)
+        float s = __fadd_rn(a.hi, a.lo);
+        float v = __fsub_rn(s, a.hi);
+        float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(a.lo, v));
+        return ff{s, e};
+    }
+    static __device__ __forceinline__ T ld(const Stor *p)
+    {
+        float2 v = *p;
+        return ff{v.x, v.y};
+    }
+    static __device__ __forceinline__ void st(Stor *p, T v) { *p = make_float2(v.hi, v.lo); }
+    static __device__ __forceinline__ T ldt(const T *p)
+    {
+        float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        return ff{v.x, v.y};
+    }
+};
+
+}  // namespace sfmm

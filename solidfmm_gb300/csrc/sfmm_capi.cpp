@@ -1,0 +1,627 @@
+// C ABI of solidfmm-gb300 (include/sfmm.h): contexts, table upload, batch
+// validation and kernel launches.  No exception crosses this boundary.
+#include "sfmm.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "sfmm_launch.hpp"
+#include "sfmm_tables.hpp"
+#include "sfmm_params.hpp"
+
+using namespace sfmm;
+
+namespace {
+
+struct DevTables {
+    void *W = nullptr, *ein_M = nullptr, *ein_L = nullptr, *eout_L = nullptr, *eout_M = nullptr;
+    void *H[3] = {nullptr, nullptr, nullptr};
+    bool ready = false;
+};
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b)
+    {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+struct HostBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b)
+    {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMallocHost(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+}  // namespace
+
+struct sfmm_context {
+    int dtype = SFMM_F64;
+    int P = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    HostTables host;
+    DevTables tab[3];  // indexed by Arith
+    std::string err;
+    uint64_t launches = 0;
+    std::mutex mtx;  // serialises host-path calls (one translator object, one stream)
+    int *d_status = nullptr;  // device error word of the translation kernels
+    // host-path staging (three pipeline slots for the packed host call)
+    DevBuf d_src[3], d_dst[3], d_meta[3], d_shift[3], d_work;
+    HostBuf h_src, h_dst, h_meta, h_shift;
+    cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+int fail(sfmm_context *c, int st, const char *fmt, ...)
+{
+    if (c) {
+        char b[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(b, sizeof b, fmt, ap);
+        va_end(ap);
+        c->err = b;
+    }
+    return st;
+}
+
+int cuda_fail(sfmm_context *c, cudaError_t e, const char *what)
+{
+    return fail(c, SFMM_CUDA_ERROR, "%s: %s", what, cudaGetErrorString(e));
+}
+
+size_t esize(Arith a) { return a == Arith::F32 ? sizeof(float) : (a == Arith::F64 ? sizeof(double) : 2 * sizeof(float)); }
+
+// convert an FP64 table into the arithmetic's element type
+std::vector<unsigned char> convert(const std::vector<double> &v, Arith a)
+{
+    std::vector<unsigned char> out(v.size() * esize(a));
+    for (size_t i = 0; i < v.size(); ++i) {
+        if (a == Arith::F64) {
+            std::memcpy(&out[i * 8], &v[i], 8);
+        } else if (a == Arith::F32) {
+            float f = (float)v[i];
+            std::memcpy(&out[i * 4], &f, 4);
+        } else {
+            float hi = (float)v[i];
+            float lo = (float)(v[i] - (double)hi);
+            std::memcpy(&out[i * 8], &hi, 4);
+            std::memcpy(&out[i * 8 + 4], &lo, 4);
+        }
+    }
+    return out;
+}
+
+cudaError_t upload(void **dst, const std::vector<double> &v, Arith a)
+{
+    auto bytes = convert(v, a);
+    cudaError_t e = cudaMalloc(dst, bytes.size() ? bytes.size() : 16);
+    if (e != cudaSuccess) return e;
+    if (bytes.empty()) return cudaSuccess;
+    return cudaMemcpy(*dst, bytes.data(), bytes.size(), cudaMemcpyHostToDevice);
+}
+
+int ensure_tables(sfmm_context *c, Arith a)
+{
+    DevTables &t = c->tab[(int)a];
+    if (t.ready) return SFMM_OK;
+    cudaError_t e;
+    if ((e = upload(&t.W, c->host.W, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+    if ((e = upload(&t.ein_M, c->host.e_in_M, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+    if ((e = upload(&t.ein_L, c->host.e_in_L, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+    if ((e = upload(&t.eout_L, c->host.e_out_L, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+    if ((e = upload(&t.eout_M, c->host.e_out_M, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+    for (int k = 0; k < 3; ++k)
+        if ((e = upload(&t.H[k], c->host.H[k], a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+    t.ready = true;
+    return SFMM_OK;
+}
+
+void free_tables(DevTables &t)
+{
+    void *ps[] = {t.W, t.ein_M, t.ein_L, t.eout_L, t.eout_M, t.H[0], t.H[1], t.H[2]};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    t = DevTables{};
+}
+
+int arith_of(sfmm_context *c, int precision, Arith *out)
+{
+    if (precision == SFMM_PLAIN) {
+        *out = c->dtype == SFMM_F64 ? Arith::F64 : Arith::F32;
+        return SFMM_OK;
+    }
+    if (precision == SFMM_SPLIT) {
+        if (c->dtype != SFMM_F64)
+            return fail(c, SFMM_UNSUPPORTED, "split precision needs an FP64 context (FP64 accumulation targets)");
+        *out = Arith::FF;
+        return SFMM_OK;
+    }
+    return fail(c, SFMM_INVALID_ARG, "unknown precision mode %d", precision);
+}
+
+// The launch itself: validated arguments, device pointers.
+int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound, long long n, const void *src,
+              long long sstride, long long nsrc, const uint32_t *sidx, void *dst, long long dstride, long long ndst,
+              const uint32_t *tidx, const uint32_t *pin, const uint32_t *pout, const double *shift,
+              const uint32_t *perm, int flags)
+{
+    if (n == 0) return SFMM_OK;
+    int st = ensure_tables(c, a);
+    if (st) return st;
+    if (Pbound < 1) Pbound = 1;
+    LaunchShape s = translate_shape(a, Pbound);
+    if (s.acc == 0) return fail(c, SFMM_UNSUPPORTED, "order %d exceeds the GPU kernels' limit %d", Pbound, kMaxKernelOrder);
+    const DevTables &t = c->tab[(int)a];
+    KParams p{};
+    p.op = op;
+    p.P = Pbound;
+    p.Ptab = c->P;
+    p.n = n;
+    p.src = src;
+    p.sstride = sstride;
+    p.nsrc = nsrc;
+    p.sidx = sidx;
+    p.dst = dst;
+    p.dstride = dstride;
+    p.ndst = ndst;
+    p.tidx = tidx;
+    p.status = c->d_status;
+    p.pin = pin;
+    p.pout = pout;
+    p.shift = shift;
+    p.perm = perm;
+    p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
+    p.W = t.W;
+    p.ein = (op == SFMM_L2L) ? t.ein_L : t.ein_M;
+    p.eout = (op == SFMM_M2M) ? t.eout_M : t.eout_L;
+    p.H = t.H[op];
+    p.spad = s.spad;
+    p.TS = s.TS;
+    long long tiles = (n + s.TS - 1) / s.TS;
+    long long grid = (long long)c->num_sms * translate_blocks_per_sm(a, s);
+    if (grid > tiles) grid = tiles;
+    cudaError_t e = launch_translate(a, p, s, (int)grid, stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "translation kernel launch");
+    c->launches++;
+    return SFMM_OK;
+}
+
+}  // namespace
+
+namespace sfmm {
+
+LaunchShape translate_shape(Arith a, int P)
+{
+    LaunchShape s;
+    if (P < 1 || P > kMaxKernelOrder) return s;
+    int acc = (P + 3) / 4;
+    acc = acc <= 2 ? 2 : (acc <= 4 ? 4 : (acc <= 6 ? 6 : 8));
+    s.acc = acc;
+    int scap = P * (P + 1);
+    s.spad = scap + ((4 - scap) % 32 + 32) % 32;
+    size_t per = (size_t)s.spad * esize(a) + 5 * sizeof(uint32_t);
+    const size_t budget = 232448;
+    int ts = (int)std::min<size_t>(64, budget / per);
+    ts = (ts / 8) * 8;
+    if (ts < 8) return LaunchShape{};
+    s.TS = ts;
+    s.threads = 4 * ts;
+    s.smem = (size_t)ts * s.spad * esize(a) + 5 * sizeof(uint32_t) * ts;
+    return s;
+}
+
+cudaError_t launch_translate_64(const KParams &, const LaunchShape &, int, cudaStream_t);
+cudaError_t launch_translate_32(const KParams &, const LaunchShape &, int, cudaStream_t);
+cudaError_t launch_translate_ff(const KParams &, const LaunchShape &, int, cudaStream_t);
+int occupancy_64(const LaunchShape &);
+int occupancy_32(const LaunchShape &);
+int occupancy_ff(const LaunchShape &);
+
+cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
+{
+    switch (a) {
+    case Arith::F64: return launch_translate_64(p, s, grid, st);
+    case Arith::F32: return launch_translate_32(p, s, grid, st);
+    default: return launch_translate_ff(p, s, grid, st);
+    }
+}
+
+int translate_blocks_per_sm(Arith a, const LaunchShape &s)
+{
+    switch (a) {
+    case Arith::F64: return occupancy_64(s);
+    case Arith::F32: return occupancy_32(s);
+    default: return occupancy_ff(s);
+    }
+}
+
+}  // namespace sfmm
+
+extern "C" {
+
+const char *sfmm_status_string(int s)
+{
+    switch (s) {
+    case SFMM_OK: return "ok";
+    case SFMM_INVALID_ARG: return "invalid argument";
+    case SFMM_ORDER_RANGE: return "order out of range";
+    case SFMM_OVERFLOW: return "order too large for the floating-point type";
+    case SFMM_DIM_MISMATCH: return "dimension mismatch";
+    case SFMM_OOM: return "out of memory";
+    case SFMM_CUDA_ERROR: return "CUDA error";
+    case SFMM_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+int sfmm_create(sfmm_context **out, int dtype, size_t P, int device)
+{
+    if (!out) return SFMM_INVALID_ARG;
+    *out = nullptr;
+    if (dtype != SFMM_F32 && dtype != SFMM_F64) return SFMM_INVALID_ARG;
+    if (P == 0) return SFMM_INVALID_ARG;
+    if ((dtype == SFMM_F32 && P > 18) || (dtype == SFMM_F64 && P > 86)) return SFMM_OVERFLOW;
+    sfmm_context *c = new (std::nothrow) sfmm_context;
+    if (!c) return SFMM_OOM;
+    c->dtype = dtype;
+    c->P = (int)P;
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        delete c;
+        return SFMM_CUDA_ERROR;
+    }
+    try {
+        c->host = build_tables((int)P);
+    } catch (const std::bad_alloc &) {
+        delete c;
+        return SFMM_OOM;
+    }
+    if (cudaMalloc(&c->d_status, sizeof(int)) != cudaSuccess || cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess) {
+        delete c;
+        return SFMM_CUDA_ERROR;
+    }
+    *out = c;
+    return SFMM_OK;
+}
+
+void sfmm_destroy(sfmm_context *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    for (auto &t : c->tab) free_tables(t);
+    for (int k = 0; k < 3; ++k) {
+        c->d_src[k].release();
+        c->d_dst[k].release();
+        c->d_meta[k].release();
+        c->d_shift[k].release();
+        if (c->pipe[k]) cudaStreamDestroy(c->pipe[k]);
+    }
+    c->d_work.release();
+    if (c->d_status) cudaFree(c->d_status);
+    c->h_src.release();
+    c->h_dst.release();
+    c->h_meta.release();
+    c->h_shift.release();
+    delete c;
+}
+
+size_t sfmm_order(const sfmm_context *c) { return c ? (size_t)c->P : 0; }
+int sfmm_data_type(const sfmm_context *c) { return c ? c->dtype : -1; }
+const char *sfmm_last_error(const sfmm_context *c) { return c ? c->err.c_str() : "null context"; }
+uint64_t sfmm_launch_count(const sfmm_context *c) { return c ? c->launches : 0; }
+
+int sfmm_set_stream(sfmm_context *c, void *stream)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    c->stream = (cudaStream_t)stream;
+    return SFMM_OK;
+}
+
+int sfmm_translate_device(sfmm_context *c, int op, int precision, size_t n, const void *src, size_t src_stride,
+                          size_t src_count, const uint32_t *src_index, void *dst, size_t dst_stride,
+                          size_t dst_count, const uint32_t *dst_index, const uint32_t *p_in, const uint32_t *p_out,
+                          const double *shift, const uint32_t *order, int flags, size_t order_bound)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    if (op < SFMM_M2M || op > SFMM_L2L) return fail(c, SFMM_INVALID_ARG, "unknown operator %d", op);
+    Arith a;
+    int st = arith_of(c, precision, &a);
+    if (st) return st;
+    if (n == 0) return SFMM_OK;
+    if (n > 0xffffffffull) return fail(c, SFMM_INVALID_ARG, "batch larger than 2^32 translations");
+    if (!src || !dst || !p_in || !p_out || !shift)
+        return fail(c, SFMM_INVALID_ARG, "null device pointer in batch");
+    size_t bound = order_bound ? order_bound : (size_t)c->P;
+    if (bound > (size_t)c->P) return fail(c, SFMM_ORDER_RANGE, "order bound %zu exceeds operator order %d", bound, c->P);
+    if (src_stride < bound * (bound + 1) || dst_stride < bound * (bound + 1))
+        return fail(c, SFMM_INVALID_ARG, "expansion stride smaller than P(P+1) for the order bound");
+    cudaSetDevice(c->device);
+    return run_batch(c, c->stream, op, a, (int)bound, (long long)n, src, (long long)src_stride,
+                     (long long)src_count, src_index, dst, (long long)dst_stride, (long long)dst_count, dst_index,
+                     p_in, p_out, shift, order, flags);
+}
+
+int sfmm_device_status(sfmm_context *c, int *flags)
+{
+    if (!c || !flags) return SFMM_INVALID_ARG;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "stream synchronise");
+    int v = 0;
+    e = cudaMemcpy(&v, c->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(c, e, "status read");
+    *flags = v;
+    return SFMM_OK;
+}
+
+int sfmm_bucket_by_order(sfmm_context *c, size_t n, const uint32_t *p_in, const uint32_t *p_out, uint32_t *order)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    if (n == 0) return SFMM_OK;
+    if (!p_in || !p_out || !order) return fail(c, SFMM_INVALID_ARG, "null device pointer");
+    cudaSetDevice(c->device);
+    cudaError_t e = c->d_work.ensure(bucket_work_words(c->P) * sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_fail(c, e, "bucket workspace");
+    e = launch_bucket((long long)n, p_in, p_out, order, (uint32_t *)c->d_work.p, c->P, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bucket kernels");
+    c->launches += 3;
+    return SFMM_OK;
+}
+
+int sfmm_p2x_device(sfmm_context *c, int kind, size_t nexp, size_t nq, const double *charge, const double *pos,
+                    const double *centre, void *out, size_t out_stride)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    if (kind != 0 && kind != 1) return fail(c, SFMM_INVALID_ARG, "kind must be 0 (P2M) or 1 (P2L)");
+    if (nexp == 0) return SFMM_OK;
+    if (!charge || !pos || !centre || !out) return fail(c, SFMM_INVALID_ARG, "null device pointer");
+    if (out_stride < (size_t)c->P * (c->P + 1)) return fail(c, SFMM_INVALID_ARG, "stride smaller than P(P+1)");
+    cudaSetDevice(c->device);
+    cudaError_t e = launch_p2x(c->dtype == SFMM_F64, kind, c->P, (long long)nexp, (long long)nq, charge, pos, centre,
+                               out, (long long)out_stride, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "P2M/P2L kernel");
+    c->launches++;
+    return SFMM_OK;
+}
+
+int sfmm_translate_host_packed(sfmm_context *c, int op, int precision, size_t n, const void *src,
+                               size_t src_stride, size_t src_count, const uint32_t *src_index, void *dst,
+                               size_t dst_stride, size_t dst_count, const uint32_t *dst_index, const uint32_t *p_in,
+                               const uint32_t *p_out, const double *shift, int flags)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    if (op < SFMM_M2M || op > SFMM_L2L) return fail(c, SFMM_INVALID_ARG, "unknown operator %d", op);
+    Arith a;
+    int st = arith_of(c, precision, &a);
+    if (st) return st;
+    if (n == 0) return SFMM_OK;
+    if (!src || !dst || !p_in || !p_out || !shift) return fail(c, SFMM_INVALID_ARG, "null host pointer in batch");
+    // checked call: validate everything before touching the targets
+    uint32_t pmax = 1;
+    for (size_t i = 0; i < n; ++i) {
+        if (p_in[i] > (uint32_t)c->P || p_out[i] > (uint32_t)c->P)
+            return fail(c, SFMM_ORDER_RANGE, "translation %zu: orders (%u,%u) exceed the operator order %d", i,
+                        p_in[i], p_out[i], c->P);
+        pmax = std::max(pmax, std::max(p_in[i], p_out[i]));
+        if (src_index && src_index[i] >= src_count) return fail(c, SFMM_INVALID_ARG, "source index out of range");
+        if (dst_index && dst_index[i] >= dst_count) return fail(c, SFMM_INVALID_ARG, "target index out of range");
+    }
+    if (!src_index && src_count < n) return fail(c, SFMM_INVALID_ARG, "fewer sources than translations");
+    if (!dst_index && dst_count < n) return fail(c, SFMM_INVALID_ARG, "fewer targets than translations");
+    if (src_stride < (size_t)pmax * (pmax + 1) || dst_stride < (size_t)pmax * (pmax + 1))
+        return fail(c, SFMM_INVALID_ARG, "expansion stride smaller than P(P+1)");
+    std::lock_guard<std::mutex> lock(c->mtx);
+    cudaSetDevice(c->device);
+    const size_t es = c->dtype == SFMM_F64 ? 8 : 4;
+    cudaError_t e;
+    for (int k = 0; k < 3; ++k)
+        if (!c->pipe[k] && (e = cudaStreamCreateWithFlags(&c->pipe[k], cudaStreamNonBlocking)) != cudaSuccess)
+            return cuda_fail(c, e, "stream create");
+    const bool pipelined = !src_index && !dst_index;
+    // chunk of translations per pipeline step
+    size_t chunk = pipelined ? std::max<size_t>(8192, (n + 23) / 24) : n;
+    if (chunk > n) chunk = n;
+    size_t nchunks = (n + chunk - 1) / chunk;
+    size_t sc = pipelined ? chunk : src_count;  // expansions per slot
+    size_t dc = pipelined ? chunk : dst_count;
+    int slots = pipelined ? (int)std::min<size_t>(3, nchunks) : 1;
+    for (int k = 0; k < slots; ++k) {
+        if ((e = c->d_src[k].ensure(sc * src_stride * es)) != cudaSuccess) return cuda_fail(c, e, "device buffers");
+        if ((e = c->d_dst[k].ensure(dc * dst_stride * es)) != cudaSuccess) return cuda_fail(c, e, "device buffers");
+        if ((e = c->d_meta[k].ensure(chunk * 4 * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(c, e, "device buffers");
+        if ((e = c->d_shift[k].ensure(chunk * 3 * sizeof(double))) != cudaSuccess) return cuda_fail(c, e, "device buffers");
+    }
+    const char *hs = (const char *)src;
+    char *hd = (char *)dst;
+    for (size_t ci = 0; ci < nchunks; ++ci) {
+        int k = (int)(ci % slots);
+        cudaStream_t s = c->pipe[k];
+        size_t b = ci * chunk, m = std::min(chunk, n - b);
+        uint32_t *dm = (uint32_t *)c->d_meta[k].p;
+        double *dsh = (double *)c->d_shift[k].p;
+        size_t ns = pipelined ? m : src_count, nd = pipelined ? m : dst_count;
+        const char *srcp = pipelined ? hs + b * src_stride * es : hs;
+        char *dstp = pipelined ? hd + b * dst_stride * es : hd;
+        if ((e = cudaMemcpyAsync(c->d_src[k].p, srcp, ns * src_stride * es, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(c->d_dst[k].p, dstp, nd * dst_stride * es, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(dm, p_in + b, m * 4, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(dm + chunk, p_out + b, m * 4, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(dsh, shift + 3 * b, m * 3 * sizeof(double), cudaMemcpyHostToDevice, s)))
+            return cuda_fail(c, e, "host-to-device copy");
+        if (src_index && (e = cudaMemcpyAsync(dm + 2 * chunk, src_index, m * 4, cudaMemcpyHostToDevice, s)))
+            return cuda_fail(c, e, "host-to-device copy");
+        if (dst_index && (e = cudaMemcpyAsync(dm + 3 * chunk, dst_index, m * 4, cudaMemcpyHostToDevice, s)))
+            return cuda_fail(c, e, "host-to-device copy");
+        st = run_batch(c, s, op, a, (int)pmax, (long long)m, c->d_src[k].p, (long long)src_stride, (long long)ns,
+                       src_index ? dm + 2 * chunk : nullptr, c->d_dst[k].p, (long long)dst_stride, (long long)nd,
+                       dst_index ? dm + 3 * chunk : nullptr, dm, dm + chunk, dsh, nullptr, flags);
+        if (st) return st;
+        if ((e = cudaMemcpyAsync(dstp, c->d_dst[k].p, nd * dst_stride * es, cudaMemcpyDeviceToHost, s)))
+            return cuda_fail(c, e, "device-to-host copy");
+    }
+    for (int k = 0; k < slots; ++k)
+        if ((e = cudaStreamSynchronize(c->pipe[k])) != cudaSuccess) return cuda_fail(c, e, "synchronise");
+    return SFMM_OK;
+}
+
+int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const void *const *src, const size_t *p_in,
+                        void *const *dst, const size_t *p_out, size_t dim, const void *x, const void *y,
+                        const void *z)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    if (op < SFMM_M2M || op > SFMM_L2L) return fail(c, SFMM_INVALID_ARG, "unknown operator %d", op);
+    Arith a;
+    int st = arith_of(c, precision, &a);
+    if (st) return st;
+    if (n == 0 || dim == 0) return SFMM_OK;
+    if (!src || !dst || !p_in || !p_out || !x || !y || !z) return fail(c, SFMM_INVALID_ARG, "null host pointer");
+    size_t pmax = 1;
+    for (size_t i = 0; i < n; ++i) {
+        if (p_in[i] > (size_t)c->P || p_out[i] > (size_t)c->P)
+            return fail(c, SFMM_ORDER_RANGE, "orders exceeding operator data (translation %zu)", i);
+        if ((p_in[i] && !src[i]) || (p_out[i] && !dst[i])) return fail(c, SFMM_INVALID_ARG, "null solid pointer");
+        pmax = std::max(pmax, std::max(p_in[i], p_out[i]));
+    }
+    const size_t es = c->dtype == SFMM_F64 ? 8 : 4;
+    const size_t stride = pmax * (pmax + 1);
+    const size_t N = n * dim;
+    // unique targets: (solid pointer, component) -> slot; sources are copied per translation
+    std::unordered_map<const void *, uint32_t> tslot;
+    std::vector<const char *> tptr;
+    std::vector<size_t> tord;
+    std::vector<uint32_t> tidx(N), pin(N), pout(N);
+    std::vector<double> sh(3 * N);
+    bool repeat = false;
+    try {
+        tslot.reserve(N);
+        for (size_t i = 0; i < n; ++i)
+            for (size_t d = 0; d < dim; ++d) {
+                size_t k = i * dim + d;
+                const char *tp = (const char *)dst[i] + d * p_out[i] * (p_out[i] + 1) * es;
+                auto it = tslot.find(tp);
+                if (it == tslot.end()) {
+                    it = tslot.emplace(tp, (uint32_t)tptr.size()).first;
+                    tptr.push_back(tp);
+                    tord.push_back(p_out[i]);
+                } else {
+                    repeat = true;
+                }
+                tidx[k] = it->second;
+                pin[k] = (uint32_t)p_in[i];
+                pout[k] = (uint32_t)p_out[i];
+                for (int j = 0; j < 3; ++j) {
+                    const void *arr = j == 0 ? x : (j == 1 ? y : z);
+                    sh[3 * k + j] = c->dtype == SFMM_F64 ? ((const double *)arr)[i] : (double)((const float *)arr)[i];
+                }
+            }
+    } catch (const std::bad_alloc &) {
+        return fail(c, SFMM_OOM, "host bookkeeping");
+    }
+    const size_t nt = tptr.size();
+    std::lock_guard<std::mutex> lock(c->mtx);
+    cudaSetDevice(c->device);
+    cudaError_t e;
+    if ((e = c->h_src.ensure(N * stride * es)) || (e = c->h_dst.ensure(nt * stride * es)))
+        return cuda_fail(c, e, "pinned staging");
+    if ((e = c->d_src[0].ensure(N * stride * es)) || (e = c->d_dst[0].ensure(nt * stride * es)) ||
+        (e = c->d_meta[0].ensure(N * 3 * sizeof(uint32_t))) || (e = c->d_shift[0].ensure(N * 3 * sizeof(double))))
+        return cuda_fail(c, e, "device buffers");
+    // gather sources (solid2buf of the whole batch) with a few host threads
+    char *hs = (char *)c->h_src.p;
+    auto gather = [&](size_t lo, size_t hi) {
+        for (size_t k = lo; k < hi; ++k) {
+            size_t i = k / dim, d = k % dim;
+            size_t cnt = p_in[i] * (p_in[i] + 1);
+            if (cnt) std::memcpy(hs + k * stride * es, (const char *)src[i] + d * cnt * es, cnt * es);
+        }
+    };
+    size_t nthr = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), N / 4096 + 1);
+    nthr = std::min<size_t>(nthr, 16);
+    if (nthr <= 1) {
+        gather(0, N);
+    } else {
+        std::vector<std::thread> th;
+        for (size_t t = 0; t < nthr; ++t) th.emplace_back(gather, N * t / nthr, N * (t + 1) / nthr);
+        for (auto &t : th) t.join();
+    }
+    uint32_t *dm = (uint32_t *)c->d_meta[0].p;
+    cudaStream_t s = c->stream;
+    if ((e = cudaMemcpyAsync(c->d_src[0].p, hs, N * stride * es, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemsetAsync(c->d_dst[0].p, 0, nt * stride * es, s)) ||
+        (e = cudaMemcpyAsync(dm, tidx.data(), N * 4, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(dm + N, pin.data(), N * 4, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(dm + 2 * N, pout.data(), N * 4, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(c->d_shift[0].p, sh.data(), N * 3 * sizeof(double), cudaMemcpyHostToDevice, s)))
+        return cuda_fail(c, e, "host-to-device copy");
+    st = run_batch(c, s, op, a, (int)pmax, (long long)N, c->d_src[0].p, (long long)stride, (long long)N, nullptr,
+                   c->d_dst[0].p, (long long)stride, (long long)nt, dm, dm + N, dm + 2 * N,
+                   (const double *)c->d_shift[0].p, nullptr, repeat ? SFMM_TARGETS_REPEAT : SFMM_TARGETS_UNIQUE);
+    if (st) return st;
+    char *hd = (char *)c->h_dst.p;
+    if ((e = cudaMemcpyAsync(hd, c->d_dst[0].p, nt * stride * es, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+        return cuda_fail(c, e, "device-to-host copy");
+    // scatter-add into the host targets (buf2solid)
+    for (size_t j = 0; j < nt; ++j) {
+        size_t cnt = tord[j] * (tord[j] + 1);
+        if (c->dtype == SFMM_F64) {
+            double *o = (double *)tptr[j];
+            const double *r = (const double *)(hd + j * stride * es);
+            for (size_t q = 0; q < cnt; ++q) o[q] += r[q];
+        } else {
+            float *o = (float *)tptr[j];
+            const float *r = (const float *)(hd + j * stride * es);
+            for (size_t q = 0; q < cnt; ++q) o[q] += r[q];
+        }
+    }
+    return SFMM_OK;
+}
+
+}  // extern "C"

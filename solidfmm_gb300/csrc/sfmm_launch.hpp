@@ -1,0 +1,42 @@
+// Host-side launch interface between the C ABI and the kernel translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace sfmm {
+
+struct KParams;
+
+enum class Arith { F64 = 0, F32 = 1, FF = 2 };
+
+// Largest order the fused translation kernel supports (accumulator arrays
+// are sized ceil(P/4) per thread).
+constexpr int kMaxKernelOrder = 32;
+
+struct LaunchShape {
+    int acc = 0;       // accumulators per thread, ceil(P/4) rounded to an instantiated size
+    int TS = 0;        // translations per CTA
+    int spad = 0;      // buffer elements per translation
+    size_t smem = 0;   // dynamic shared memory bytes
+    int threads = 0;   // 4 * TS
+};
+
+LaunchShape translate_shape(Arith a, int P);
+
+// Launch the fused translation kernel (defined in sfmm_k{64,32,ff}.cu).
+cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, int grid, cudaStream_t st);
+int translate_blocks_per_sm(Arith a, const LaunchShape &s);
+
+// P2M / P2L (sfmm_p2x.cu)
+cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const double *q,
+                       const double *pos, const double *centre, void *out, long long stride, cudaStream_t st);
+
+// bucketing by order pair (sfmm_p2x.cu)
+cudaError_t launch_bucket(long long n, const uint32_t *pin, const uint32_t *pout, uint32_t *order,
+                          uint32_t *work, int P, cudaStream_t st);
+size_t bucket_work_words(int P);
+
+}  // namespace sfmm

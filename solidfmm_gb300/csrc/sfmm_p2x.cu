@@ -1,0 +1,180 @@
+// P2M / P2L expansion building and order bucketing.
+//
+// P2M/P2L: out[j] += sum_k q_jk * R(x_jk - c_j) (or S), the reference's
+// fmadd(q, harmonics::R/S(P, x - c), E) (solid.cpp:70-104) with the R and S
+// recurrences of harmonics.cpp:32-80 and :177-224, evaluated column by column
+// (fixed m, increasing n) so that each coefficient is accumulated as soon as
+// it is produced.  One thread per expansion, FP64 arithmetic.
+//
+// Bucketing: a counting sort of translation indices by the key
+// (p_in, p_out), so that warps see uniform orders.
+#include <algorithm>
+#include <cstdint>
+
+#include "sfmm_launch.hpp"
+
+namespace sfmm {
+
+template <class Out>
+__global__ void k_p2x(int kind, int P, long long nexp, long long nq, const double *__restrict__ q,
+                      const double *__restrict__ pos, const double *__restrict__ centre, Out *out, long long stride)
+{
+    long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= nexp) return;
+    Out *o = out + j * stride;
+    const double cx = centre[3 * j], cy = centre[3 * j + 1], cz = centre[3 * j + 2];
+    for (long long k = 0; k < nq; ++k) {
+        const double w = q[j * nq + k];
+        const double *pp = pos + 3 * (j * nq + k);
+        const double x = pp[0] - cx, y = pp[1] - cy, z = pp[2] - cz;
+        const double r2 = x * x + y * y + z * z;
+        if (kind == 0) {
+            // regular harmonics R
+            double dr = 1.0, di = 0.0;  // R(m,m)
+            for (int m = 0; m < P; ++m) {
+                if (m > 0) {
+                    double f = (m == 1) ? 0.5 : 1.0 / (2.0 * m);
+                    double nr = (dr * x - di * y) * f;
+                    double ni = (dr * y + di * x) * f;
+                    dr = nr;
+                    di = ni;
+                }
+                // column m: R(m,m), R(m+1,m) = z R(m,m), then the three-term recurrence
+                double ar = dr, ai = di;            // R(n-1,m)
+                double br = 0.0, bi = 0.0;          // R(n-2,m)
+                o[m * (m + 1) + m] += (Out)(w * ar);
+                o[(m + 1) * (m + 1) + m] += (Out)(w * ai);
+                for (int n = m + 1; n < P; ++n) {
+                    double cr, ci;
+                    if (n == m + 1) {
+                        cr = z * ar;
+                        ci = z * ai;
+                    } else {
+                        double f = 1.0 / ((double)(n + m) * (double)(n - m));
+                        cr = (ar * z * (2 * n - 1) - r2 * br) * f;
+                        ci = (ai * z * (2 * n - 1) - r2 * bi) * f;
+                    }
+                    o[n * (n + 1) + m] += (Out)(w * cr);
+                    o[(n + 1) * (n + 1) + m] += (Out)(w * ci);
+                    br = ar;
+                    bi = ai;
+                    ar = cr;
+                    ai = ci;
+                }
+            }
+        } else {
+            // singular harmonics S
+            const double r2inv = 1.0 / r2;
+            double dr = sqrt(r2inv), di = 0.0;  // S(m,m)
+            for (int m = 0; m < P; ++m) {
+                if (m > 0) {
+                    double f = (2.0 * m - 1.0) * r2inv;
+                    double nr = (dr * x - di * y) * f;
+                    double ni = (dr * y + di * x) * f;
+                    dr = nr;
+                    di = ni;
+                }
+                double ar = dr, ai = di, br = 0.0, bi = 0.0;
+                o[m * (m + 1) + m] += (Out)(w * ar);
+                o[(m + 1) * (m + 1) + m] += (Out)(w * ai);
+                for (int n = m + 1; n < P; ++n) {
+                    double cr, ci;
+                    if (n == m + 1) {
+                        double f = (2.0 * m + 1.0) * z * r2inv;
+                        cr = f * ar;
+                        ci = f * ai;
+                    } else {
+                        double c2 = (double)(n + m - 1) * (double)(n - m - 1);
+                        cr = (ar * z * (2 * n - 1) - c2 * br) * r2inv;
+                        ci = (ai * z * (2 * n - 1) - c2 * bi) * r2inv;
+                    }
+                    o[n * (n + 1) + m] += (Out)(w * cr);
+                    o[(n + 1) * (n + 1) + m] += (Out)(w * ci);
+                    br = ar;
+                    bi = ai;
+                    ar = cr;
+                    ai = ci;
+                }
+            }
+        }
+    }
+}
+
+cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const double *q, const double *pos,
+                       const double *centre, void *out, long long stride, cudaStream_t st)
+{
+    if (nexp == 0) return cudaSuccess;
+    int tb = 128;
+    long long grid = (nexp + tb - 1) / tb;
+    if (f64)
+        k_p2x<double><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, q, pos, centre, (double *)out, stride);
+    else
+        k_p2x<float><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, q, pos, centre, (float *)out, stride);
+    return cudaGetLastError();
+}
+
+// ---- bucketing by (p_in, p_out) ----
+
+__global__ void k_bucket_count(long long n, const uint32_t *pin, const uint32_t *pout, uint32_t *cnt, int K)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        uint32_t key = min(pin[i], (uint32_t)(K - 1)) * (uint32_t)K + min(pout[i], (uint32_t)(K - 1));
+        atomicAdd(&cnt[key], 1u);
+    }
+}
+
+// single CTA exclusive scan over K*K counters (K <= 33)
+__global__ void k_bucket_scan(uint32_t *cnt, int nkeys)
+{
+    __shared__ uint32_t part[1024];
+    const int t = threadIdx.x;
+    const int per = (nkeys + blockDim.x - 1) / blockDim.x;
+    uint32_t s = 0;
+    for (int k = t * per; k < min(nkeys, (t + 1) * per); ++k) s += cnt[k];
+    part[t] = s;
+    __syncthreads();
+    if (t == 0) {
+        uint32_t run = 0;
+        for (int k = 0; k < (int)blockDim.x; ++k) {
+            uint32_t v = part[k];
+            part[k] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    uint32_t run = part[t];
+    for (int k = t * per; k < min(nkeys, (t + 1) * per); ++k) {
+        uint32_t v = cnt[k];
+        cnt[k] = run;
+        run += v;
+    }
+}
+
+__global__ void k_bucket_scatter(long long n, const uint32_t *pin, const uint32_t *pout, uint32_t *off, int K,
+                                 uint32_t *order)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        uint32_t key = min(pin[i], (uint32_t)(K - 1)) * (uint32_t)K + min(pout[i], (uint32_t)(K - 1));
+        uint32_t pos = atomicAdd(&off[key], 1u);
+        order[pos] = (uint32_t)i;
+    }
+}
+
+size_t bucket_work_words(int P) { return (size_t)(P + 1) * (P + 1); }
+
+cudaError_t launch_bucket(long long n, const uint32_t *pin, const uint32_t *pout, uint32_t *order, uint32_t *work,
+                          int P, cudaStream_t st)
+{
+    const int K = P + 1;
+    const int nkeys = K * K;
+    cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t) * nkeys, st);
+    if (e != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    int grid = (int)std::min<long long>((n + 255) / 256, 4096);
+    k_bucket_count<<<grid, 256, 0, st>>>(n, pin, pout, work, K);
+    k_bucket_scan<<<1, 1024, 0, st>>>(work, nkeys);
+    k_bucket_scatter<<<grid, 256, 0, st>>>(n, pin, pout, work, K, order);
+    return cudaGetLastError();
+}
+
+}  // namespace sfmm

@@ -1,0 +1,38 @@
+// Kernel parameter block shared by the C ABI (host C++) and the kernels.
+#pragma once
+
+#include <cstdint>
+
+namespace sfmm {
+
+enum { OP_M2M = 0, OP_M2L = 1, OP_L2L = 2 };
+
+struct KParams {
+    int op;
+    int P;          // order bound of this batch: every p_in/p_out <= P
+    int Ptab;       // order the tables were built for (>= P)
+    long long n;
+    const void *src;
+    long long sstride;
+    long long nsrc;     // expansions addressable through src
+    const uint32_t *sidx;
+    void *dst;
+    long long dstride;
+    long long ndst;     // expansions addressable through dst
+    const uint32_t *tidx;
+    const uint32_t *pin;
+    const uint32_t *pout;
+    const double *shift;
+    const uint32_t *perm;
+    int atomic;
+    const void *W;      // arith-typed swap matrices
+    const void *ein;    // arith-typed forward edge factors (op dependent)
+    const void *eout;   // arith-typed backward edge factors (op dependent)
+    const void *H;      // arith-typed z matrices of this op
+    int spad;           // buffer elements per translation
+    int TS;             // translations per CTA tile
+    void *scratch;      // global buffer (GBUF kernels)
+    int *status;        // device error word: bit 0 = a translation had an out-of-range index or order
+};
+
+}  // namespace sfmm

@@ -1,0 +1,48 @@
+// Host-side operator tables for the GPU translation kernels.
+//
+// Plays the role of the reference's operator_data<real> (factorials and the
+// packed real/imag swap matrices, solidfmm/operator_data.cpp:48-244), built
+// once per context in FP64 and uploaded.  The kernels work in an orthogonal
+// basis of each degree-n subspace:
+//
+//   D_m   = sqrt((n-m)! (n+m)!),   s_0 = sqrt(2), s_m = 1 (m > 0)
+//   E_m   = D_m / s_m,             F_m = D_m * s_m
+//   W_R   = E Rf E^-1 = F^-1 Rt F  (Rf, Rt: the reference's real swap matrix and its
+//                                   transposed variant, operator_data.cpp:48-122)
+//   W_I   = D If D^-1 = D^-1 It D  (imag swap matrix, operator_data.cpp:74-147)
+//
+// W_R and W_I are orthogonal, symmetric involutions with entries |w| <= 1, so
+// both the forward (Rf) and backward (Rt) swaps use the same W.  The diagonal
+// scalings are folded into the edge factors (first and last rotation of each
+// degree) and into the z-translation matrices H_m.
+#pragma once
+
+#include <cstddef>
+#include <vector>
+
+namespace sfmm {
+
+struct HostTables {
+    int P = 0;
+    // W for degree n: R block at woff[n], I block at woff[n] + d*d, both
+    // column-major: entry (row i, column j) at j*d + i, d = n+1.
+    std::vector<double> W;
+    std::vector<size_t> woff;
+    // Edge factors indexed n(n+1)/2 + m:
+    std::vector<double> e_in_M;   // E^(n)_m        forward of M2M/M2L inputs
+    std::vector<double> e_in_L;   // 1 / F^(n)_m    forward of L2L inputs
+    std::vector<double> e_out_L;  // F^(n)_m        backward of M2L/L2L outputs
+    std::vector<double> e_out_M;  // 1 / E^(n)_m    backward of M2M outputs
+    // z-translation matrices per op (0 M2M, 1 M2L, 2 L2L) and column m:
+    // entry (output n', input k) at hoff[m] + (k-m)*(P-m) + (n'-m).
+    std::vector<double> H[3];
+    std::vector<size_t> hoff;
+};
+
+// Dehnen's swap matrix B_n^{m,l} (swap_matrix.cpp:149-171), all n < P,
+// stored per n as (2n+1)^2 with (m,l) at (m+n) + (l+n)(2n+1).
+std::vector<std::vector<double>> swap_matrices(int P);
+
+HostTables build_tables(int P);
+
+}  // namespace sfmm

@@ -1,0 +1,97 @@
+"""Shared helpers for the tests: error metrics, golden-case loading, and a
+runner that pushes a batch through the C ABI (device path) with torch
+tensors as device memory."""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+
+GOLDEN = os.path.join(ROOT, "tests", "golden", "translations.npz")
+
+
+def S_of(P: int) -> int:
+    return P * (P + 1)
+
+
+def norm_weights(P: int, kind: str) -> np.ndarray:
+    """Weights turning solid coefficients of order P into the orthonormal
+    (Schmidt) basis: L / sqrt((n-m)!(n+m)!) for locals, M * sqrt(...) for
+    multipoles.  In that basis the squared L2 norm of an expansion is the
+    squared L2 norm of its field over the unit sphere (up to a constant)."""
+    w = np.ones(S_of(P))
+    for n in range(P):
+        for m in range(n + 1):
+            d = math.sqrt(math.factorial(n - m) * math.factorial(n + m))
+            f = d if kind == "M" else 1.0 / d
+            w[n * (n + 1) + m] = f
+            w[(n + 1) * (n + 1) + m] = f
+    return w
+
+
+def rel_err(got, ref, weights=None):
+    """max over rows of the relative L2 error (optionally weighted)."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    if weights is not None:
+        got = got * weights[: got.shape[-1]]
+        ref = ref * weights[: ref.shape[-1]]
+    num = np.linalg.norm(got - ref, axis=-1)
+    den = np.linalg.norm(ref, axis=-1)
+    ok = den > 0
+    if not ok.any():
+        return float(np.max(num))
+    return float(np.max(num[ok] / den[ok]))
+
+
+def per_degree_err(got, ref, P, weights=None):
+    out = []
+    for n in range(P):
+        idx = list(range(n * (n + 1), n * (n + 1) + n + 1)) + list(range((n + 1) ** 2, (n + 1) ** 2 + n + 1))
+        g = np.asarray(got)[..., idx]
+        r = np.asarray(ref)[..., idx]
+        if weights is not None:
+            g = g * weights[idx]
+            r = r * weights[idx]
+        num = np.linalg.norm(g - r, axis=-1)
+        den = np.linalg.norm(r, axis=-1)
+        ok = den > 0
+        out.append(float(np.max(num[ok] / den[ok])) if ok.any() else 0.0)
+    return out
+
+
+def load_golden():
+    z = np.load(GOLDEN)
+    cases = {}
+    for k in z.files:
+        name, field = k.split("/")
+        cases.setdefault(name, {})[field] = z[k]
+    return cases
+
+
+def run_device(ctx, op, precision, src, dst0, Pin, Pout, xyz, sidx=None, tidx=None, repeat=False, order=None,
+               order_bound=0):
+    """dst0 + T(src) computed on the GPU through sfmm_translate_device."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    dt = torch.float64 if src.dtype == np.float64 else torch.float32
+    s = torch.as_tensor(np.ascontiguousarray(src), dtype=dt, device=dev)
+    d = torch.as_tensor(np.ascontiguousarray(dst0), dtype=dt, device=dev)
+    pi = torch.as_tensor(np.asarray(Pin, np.uint32).astype(np.int32), device=dev)
+    po = torch.as_tensor(np.asarray(Pout, np.uint32).astype(np.int32), device=dev)
+    sh = torch.as_tensor(np.ascontiguousarray(xyz, np.float64), device=dev)
+    si = None if sidx is None else torch.as_tensor(np.asarray(sidx, np.uint32).astype(np.int32), device=dev)
+    ti = None if tidx is None else torch.as_tensor(np.asarray(tidx, np.uint32).astype(np.int32), device=dev)
+    od = None if order is None else torch.as_tensor(np.asarray(order, np.uint32).astype(np.int32), device=dev)
+    ctx.translate_device(op, precision, len(Pin), s, s.shape[-1], s.shape[0], d, d.shape[-1], d.shape[0], pi, po, sh,
+                         src_index=si, dst_index=ti, order=od, repeat=repeat, order_bound=order_bound)
+    torch.cuda.synchronize()
+    assert ctx.device_status() == 0
+    return d.cpu().numpy()
