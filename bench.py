@@ -1,0 +1,400 @@
+"""Benchmark: M2L translations/s at P=16 (2,000,000 translations), the
+split-precision ("chosen") path against the plain FP64 GPU path, with
+relative error against the FP64 naive oracle and roofline fractions.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload m2l16|m2l10|m2m20|l2l20|m2l20]
+
+One step = one pass of the translation kernel over the whole batch.  Inputs
+are synthetic with the benchmark's geometry: each source multipole comes from
+64 unit charges of random sign uniform in a ball of radius 0.5 (P2M on the
+GPU), each target centre lies at distance U[2,4] in a uniform direction.
+The batch (src + dst = 8.7 GB in FP64) is far larger than L2 (129 MB), so no
+flush is needed between steps.  With --gpus N > 1 every rank runs an
+independent replica of the batch (translations are independent; no
+collective), reported as weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (op, P, N, charges per source)
+    "m2l16": ("m2l", 16, 2_000_000, 64),
+    "m2l10": ("m2l", 10, 100_000, 64),
+    "m2l20": ("m2l", 20, 1_000_000, 128),
+    "m2m20": ("m2m", 20, 1_000_000, 128),
+    "l2l20": ("l2l", 20, 1_000_000, 128),
+}
+
+METRIC = "M2L translations/s at P=16, chosen vs plain FP64 GPU at equal rel. error; %roofline"
+
+
+def useful_flops(op, P):
+    """Algorithmic flops of one translation (rotations + z-translation), equal orders."""
+    rot = 2 * sum(4 * d * d + 16 * d for d in range(1, P + 1))
+    if op == "m2l":
+        z = sum(4 * (P - m) * (P - m) for m in range(P))
+    else:
+        z = sum(2 * (P - m) * (P - m + 1) for m in range(P))
+    return rot + z
+
+
+def algorithmic_bytes(P, esize=8):
+    """HBM bytes of one translation: read source, read+write target, FP64 shift."""
+    S = P * (P + 1)
+    return esize * 3 * S + 24
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = []
+        mx = 0.0
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx = max(mx, float(s[2]))
+                for nm, v in zip(names, s[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if args.impl != "reference" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(world, v, device):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_inputs(ctx, op, P, N, nq, seed, dev):
+    """Sources by P2M/P2L on the GPU (FP64), shifts, orders."""
+    import torch
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    S = P * (P + 1)
+    src = torch.zeros(N, S, dtype=torch.float64, device=dev)
+    chunk = 250_000
+    for b in range(0, N, chunk):
+        m = min(chunk, N - b)
+        d = torch.randn(m, nq, 3, dtype=torch.float64, device=dev, generator=g)
+        d = d / d.norm(dim=2, keepdim=True)
+        rr = 0.5 * torch.rand(m, nq, 1, dtype=torch.float64, device=dev, generator=g) ** (1.0 / 3.0)
+        pos = d * rr
+        q = torch.randint(0, 2, (m, nq), device=dev, generator=g).to(torch.float64) * 2 - 1
+        cen = torch.zeros(m, 3, dtype=torch.float64, device=dev)
+        if op == "l2l":  # local inputs: P2L of a cloud at distance U[2,4]
+            u = torch.randn(m, 3, dtype=torch.float64, device=dev, generator=g)
+            u = u / u.norm(dim=1, keepdim=True)
+            pos = pos + (u * (2 + 2 * torch.rand(m, 1, dtype=torch.float64, device=dev, generator=g)))[:, None, :]
+        ctx.p2x(1 if op == "l2l" else 0, m, nq, q.contiguous(), pos.contiguous(), cen, src[b:b + m], S)
+    if op == "m2l":
+        u = torch.randn(N, 3, dtype=torch.float64, device=dev, generator=g)
+        u = u / u.norm(dim=1, keepdim=True)
+        shift = u * (2 + 2 * torch.rand(N, 1, dtype=torch.float64, device=dev, generator=g))
+    else:
+        shift = 0.5 * (torch.randint(0, 2, (N, 3), device=dev, generator=g).to(torch.float64) * 2 - 1)
+    pin = torch.full((N,), P, dtype=torch.int32, device=dev)
+    return src, shift.contiguous(), pin
+
+
+def accuracy(ctx, op, P, src, shift, pin, nsub, dev):
+    """Relative errors of the plain FP64 and split paths against the naive
+    FP64 oracle on the first nsub translations (orthonormal basis and raw)."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle
+    from helpers import norm_weights, per_degree_err, rel_err
+
+    S = P * (P + 1)
+    s = src[:nsub].contiguous()
+    sh = shift[:nsub].contiguous()
+    pi = pin[:nsub].contiguous()
+    s_h = s.cpu().numpy()
+    ref = np.zeros((nsub, S))
+    pyoracle.naive(op, s_h, pi.cpu().numpy().astype(np.uint32), ref, pi.cpu().numpy().astype(np.uint32),
+                   sh.cpu().numpy())
+    w = norm_weights(P, "M" if op == "m2m" else "L")
+    out = {}
+    for name, prec in (("plain_fp64", 0), ("split", 1)):
+        d = torch.zeros(nsub, S, dtype=torch.float64, device=dev)
+        ctx.translate_device(op, prec, nsub, s, S, nsub, d, S, nsub, pi, pi, sh)
+        torch.cuda.synchronize()
+        got = d.cpu().numpy()
+        out[name] = {"rel_l2_orthonormal_max": rel_err(got, ref, w), "rel_l2_raw_max": rel_err(got, ref),
+                     "rel_l2_orthonormal_per_degree_max": per_degree_err(got, ref, P, w)}
+    return out
+
+
+def cpu_leg(op, P, nq, seconds_target, seed, use_ref):
+    """Reference (or oracle port) CPU translations on a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    rng = np.random.default_rng(seed)
+    ns = 20_000 if P >= 16 else 50_000
+    S = P * (P + 1)
+    # sample inputs: random expansions with the workload's magnitudes are not
+    # needed for timing; zero-valued solids as in the reference's benchmarks
+    src = rng.standard_normal((ns, S)) * 1e-3
+    dst = np.zeros((ns, S))
+    u = rng.standard_normal((ns, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    shift = u * rng.uniform(2, 4, (ns, 1))
+    pin = np.full(ns, P, np.uint32)
+    idx = np.arange(ns, dtype=np.uint32)
+    threads = os.cpu_count() or 1
+    total = 0.0
+    done = 0
+    while total < seconds_target:
+        if use_ref:
+            total += pyoracle.reference(op, P, src, pin, dst, pin, shift, idx, idx, mode=3, native=True)
+        else:
+            total += pyoracle.rot(op, src, pin, dst, pin, shift, nthreads=threads)
+        done += ns
+    return done / total, threads, ns, done
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="m2l16", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    op, P, N, nq = WORKLOADS[args.workload]
+    world, rank, local = dist_init(args)
+    config = {"workload": f"{op.upper()} P={P} (reference order: degrees 0..{P - 1}), {N} translations per GPU, "
+                          f"{nq} charges per source, FP64 expansions",
+              "op": op, "P": P, "translations": N, "charges_per_source": nq,
+              "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+
+        use_ref = pyoracle.ref_available()
+        kind = "reference" if use_ref else "port"
+        vals = []
+        for i in range(args.warmup + args.steps):
+            v, threads, ns, done = cpu_leg(op, P, nq, 2.0, 1000 + i, use_ref)
+            if i >= args.warmup:
+                vals.append(v)
+        value = statistics.median(vals)
+        line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "translations/s", "n_gpus": 1,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * ns / value,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": value, "unit": "translations/s", "cores": threads, "kind": kind,
+                                 "sample": f"{ns} {op.upper()} translations at P={P} per pass, repeated >= 2 s "
+                                           f"per step, {'reference multithreaded_translator::m2l_unchecked' if use_ref else 'oracle port of the rotation-based driver, one pthread per core'}"},
+                "e2e": {"value": value, "unit": "translations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    import solidfmm_gb300 as sf
+    from solidfmm_gb300 import build as _b
+
+    _b.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = sf.Context(P, "f64", device=local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    src, shift, pin = make_inputs(ctx, op, P, N, nq, 1234 + rank, dev)
+    S = P * (P + 1)
+    dst = torch.zeros(N, S, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+
+    L = sf.load()
+    L.sfmm_measure_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    peaks = {}
+    for fp64, nm in ((1, "fp64"), (0, "fp32")):
+        v = C.c_double(0)
+        L.sfmm_measure_fma_peak(fp64, local, C.byref(v))
+        peaks[nm] = v.value
+
+    def run(prec):
+        ctx.translate_device(op, prec, N, src, S, N, dst, S, N, pin, pin, shift)
+
+    def timed(prec, steps, warmup, clocks=None):
+        for _ in range(warmup):
+            run(prec)
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        l0 = ctx.launches
+        if clocks:
+            clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            run(prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        clk = clocks.stop() if clocks else None
+        ms = e0.elapsed_time(e1) / steps
+        return allmax(world, ms, dev), ctx.launches - l0, clk
+
+    clocks = Clocks(local)
+    ms_split, launches, clk = timed(1, args.steps, args.warmup, clocks)
+    ms_plain, _, _ = timed(0, max(2, args.steps // 2), 1)
+    value = world * N / (ms_split * 1e-3)
+    plain_value = world * N / (ms_plain * 1e-3)
+
+    # end to end through the C ABI with pinned host buffers
+    h_src = torch.empty(N, S, dtype=torch.float64, pin_memory=True)
+    h_src.copy_(src)
+    h_dst = torch.zeros(N, S, dtype=torch.float64, pin_memory=True)
+    h_pin = pin.cpu().numpy().astype(np.uint32)
+    h_shift = shift.cpu().numpy()
+    e2e_steps = max(2, args.steps // 2)
+    ctx.translate_host_packed(op, 1, h_src, h_dst, h_pin, h_pin, h_shift)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.translate_host_packed(op, 1, h_src, h_dst, h_pin, h_pin, h_shift)
+    t1 = time.perf_counter()
+    e2e_s = allmax(world, (t1 - t0) / e2e_steps, dev)
+    h2d = N * S * 8 * 2 + N * 8 + N * 24
+    d2h = N * S * 8
+
+    acc = accuracy(ctx, op, P, src, shift, pin, 1000, dev) if rank == 0 else None
+
+    if rank != 0:
+        return
+    F = useful_flops(op, P)
+    B = algorithmic_bytes(P)
+    t_kernel = ms_split * 1e-3 / N  # seconds per translation (one launch per step)
+    achieved_gbs = B / t_kernel / 1e9
+    hbm_peak = 6747.3
+    mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak_src = "fallback"
+    if os.path.exists(mp):
+        with open(mp) as f:
+            hbm_peak = json.load(f).get("hbm_gbs", hbm_peak)
+        peak_src = "measured"
+    roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_source": peak_src,
+            "kernel": "k_translate<ff,4> (split)", "bytes_per_translation": B}
+    ff_ops_per_flop = 5.5  # float-float multiply-add: 11 FP32 operations for 2 flops
+    roof_compute = {
+        "pipe": "fp32 (float-float arithmetic)",
+        "useful_flops_per_translation": F,
+        "fp32_ops_per_translation": F * ff_ops_per_flop,
+        "achieved_tflops": F * ff_ops_per_flop / t_kernel / 1e12,
+        "peak_tflops": peaks["fp32"] / 1e12, "peak_source": "measured FFMA loop in this run",
+        "frac": F * ff_ops_per_flop / t_kernel / peaks["fp32"]}
+    roof_fp64 = {"kernel": "k_translate<double,4> (plain FP64)", "pipe": "fp64",
+                 "achieved_tflops": F * plain_value / world / 1e12, "peak_tflops": peaks["fp64"] / 1e12,
+                 "frac": F * plain_value / world / peaks["fp64"], "peak_source": "measured DFMA loop in this run"}
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+
+        use_ref = pyoracle.ref_available()
+        v, threads, ns, done = cpu_leg(op, P, nq, args.cpu_seconds, 99, use_ref)
+        cpu = {"value": v, "unit": "translations/s", "cores": threads, "kind": "reference" if use_ref else "port",
+               "sample": f"{done} {op.upper()} translations at P={P} in passes of {ns}, FP64, "
+                         f"{'reference multithreaded_translator' if use_ref else 'oracle port, one pthread per core'}"}
+    line = {"metric": METRIC, "value": value, "unit": "translations/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_split, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32x2 (float-float) swaps/rotations/z-translation, f64 geometry and "
+                                          "accumulation", "data": "synthetic (seeded P2M of random charges)",
+            "config": config,
+            "plain_fp64": {"value": plain_value, "ms_per_step": ms_plain},
+            "split_over_plain_fp64": value / plain_value,
+            "accuracy_vs_fp64_oracle_1000": acc,
+            "e2e": {"value": world * N / e2e_s, "unit": "translations/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "api": "sfmm_translate_host_packed (pinned host buffers)"},
+            "roofline": roof, "roofline_compute": roof_compute, "roofline_plain_fp64": roof_fp64,
+            "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

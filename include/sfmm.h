@@ -137,6 +137,14 @@ int sfmm_bucket_by_order(sfmm_context *ctx, size_t n, const uint32_t *p_in, cons
 int sfmm_p2x_device(sfmm_context *ctx, int kind, size_t nexp, size_t nq, const double *charge,
                     const double *pos, const double *centre, void *out, size_t out_stride);
 
+/* Diagnostics: measured FMA-pipe throughput (flop/s, 2 per FMA) of the
+ * device, FP64 (fp64 = 1) or FP32 (fp64 = 0); the roofline denominator of
+ * the plain FP64 and split-precision kernels. */
+int sfmm_measure_fma_peak(int fp64, int device, double *flops_per_second);
+/* Diagnostics: measured throughput of 32x32->64-bit integer multiply-adds
+ * (operations/s, one per multiply-add). */
+int sfmm_measure_imad_peak(int device, double *ops_per_second);
+
 /* Number of kernel launches issued by this context since creation. */
 uint64_t sfmm_launch_count(const sfmm_context *ctx);
 

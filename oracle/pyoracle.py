@@ -17,7 +17,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
-REF_LIB = os.path.join(HERE, "_ref", os.environ.get("SFMM_REF_LIB", "libsolidfmm_ref_generic.so"))
+# generic-microkernel build: the correctness checker (bit-identical to the
+# portable C++ kernels); native build: the reference's own SIMD dispatch, used
+# for timing (its AVX-512F double kernel mishandles lanes 12-15 of a batch).
+REF_LIB = os.path.join(HERE, "_ref", "libsolidfmm_ref_generic.so")
+REF_LIB_NATIVE = os.path.join(HERE, "_ref", "libsolidfmm_ref.so")
 REF_SRC = "/root/reference"
 
 OPS = {"m2m": 0, "m2l": 1, "l2l": 2}
@@ -37,7 +41,7 @@ def build(with_ref: bool | None = None) -> None:
 
 
 _lib = None
-_ref = None
+_ref = {}
 
 
 def lib():
@@ -67,10 +71,10 @@ def ref_available() -> bool:
     return os.path.exists(REF_LIB)
 
 
-def ref():
-    global _ref
-    if _ref is None:
-        L = C.CDLL(REF_LIB)
+def ref(native=False):
+    path = REF_LIB_NATIVE if native else REF_LIB
+    if path not in _ref:
+        L = C.CDLL(path)
         for f, fp in ((L.ref_translate_d, _f64p), (L.ref_translate_f, _f32p)):
             f.argtypes = [C.c_int, C.c_size_t, C.c_size_t, C.c_size_t, fp, _u32p, C.c_size_t, C.c_size_t, fp,
                           _u32p, C.c_size_t, _u32p, _u32p, fp, C.c_size_t, C.c_int, C.POINTER(C.c_double)]
@@ -81,8 +85,8 @@ def ref():
         L.ref_swap_B.restype = C.c_double
         L.ref_dot_d.argtypes = [C.c_size_t, C.c_size_t, _f64p, C.c_size_t, C.c_size_t, _f64p, _f64p]
         L.ref_hw_threads.restype = C.c_uint
-        _ref = L
-    return _ref
+        _ref[path] = L
+    return _ref[path]
 
 
 def S_of(P: int) -> int:
@@ -141,10 +145,10 @@ class RefError(Exception):
         self.code = code
 
 
-def reference(op, Pop, src, Psrc, dst, Ptgt, xyz, sidx, tidx, dim=1, mode=0):
+def reference(op, Pop, src, Psrc, dst, Ptgt, xyz, sidx, tidx, dim=1, mode=0, native=False):
     """dst += T(src) through the reference library's own API; returns seconds."""
     op = OPS.get(op, op)
-    R = ref()
+    R = ref(native)
     f = R.ref_translate_d if src.dtype == np.float64 else R.ref_translate_f
     sec = C.c_double(0)
     rc = f(op, Pop, len(sidx), src.shape[0], src.reshape(-1), _u32(Psrc), src.shape[-1], dst.shape[0],

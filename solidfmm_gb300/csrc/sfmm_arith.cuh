@@ -25,6 +25,7 @@ struct arith;
 
 template <>
 struct arith<double> {
+    static constexpr bool split = false;
     using T = double;
     using Stor = double;  // element type of the shared-memory buffer
     using Acc = double;
@@ -41,10 +42,13 @@ struct arith<double> {
     static __device__ __forceinline__ T ld(const Stor *p) { return *p; }
     static __device__ __forceinline__ void st(Stor *p, T v) { *p = v; }
     static __device__ __forceinline__ T ldt(const T *p) { return __ldg(p); }
+    // a1*b1 + a2*b2
+    static __device__ __forceinline__ T dot2(T a1, T b1, T a2, T b2) { return fma(a1, b1, a2 * b2); }
 };
 
 template <>
 struct arith<float> {
+    static constexpr bool split = false;
     using T = float;
     using Stor = float;
     using Acc = float;
@@ -61,6 +65,7 @@ struct arith<float> {
     static __device__ __forceinline__ T ld(const Stor *p) { return *p; }
     static __device__ __forceinline__ void st(Stor *p, T v) { *p = v; }
     static __device__ __forceinline__ T ldt(const T *p) { return __ldg(p); }
+    static __device__ __forceinline__ T dot2(T a1, T b1, T a2, T b2) { return fmaf(a1, b1, a2 * b2); }
 };
 
 // Fast2Sum: |a| >= |b| assumed (or a == 0)
@@ -105,6 +110,7 @@ struct ffacc {
 
 template <>
 struct arith<ff> {
+    static constexpr bool split = true;
     using T = ff;
     using Stor = float2;
     using Acc = ffacc;
@@ -147,6 +153,23 @@ struct arith<ff> {
     {
         float2 v = __ldg(reinterpret_cast<const float2 *>(p));
         return ff{v.x, v.y};
+    }
+    // a1*b1 + a2*b2 with both products split exactly and one TwoSum (19 FP32 operations)
+    static __device__ __forceinline__ T dot2(T a1, T b1, T a2, T b2)
+    {
+        float p1 = __fmul_rn(a1.hi, b1.hi);
+        float e1 = __fmaf_rn(a1.hi, b1.hi, -p1);
+        e1 = __fmaf_rn(a1.hi, b1.lo, e1);
+        e1 = __fmaf_rn(a1.lo, b1.hi, e1);
+        float p2 = __fmul_rn(a2.hi, b2.hi);
+        float e2 = __fmaf_rn(a2.hi, b2.hi, -p2);
+        e2 = __fmaf_rn(a2.hi, b2.lo, e2);
+        e2 = __fmaf_rn(a2.lo, b2.hi, e2);
+        float s = __fadd_rn(p1, p2);
+        float v = __fsub_rn(s, p1);
+        float t = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v));
+        t = __fadd_rn(t, __fadd_rn(e1, e2));
+        return ff_norm(s, t);
     }
 };
 

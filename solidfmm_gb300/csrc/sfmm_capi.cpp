@@ -8,8 +8,10 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -91,6 +93,8 @@ struct sfmm_context {
     DevBuf d_src[3], d_dst[3], d_meta[3], d_shift[3], d_work;
     HostBuf h_src, h_dst, h_meta, h_shift;
     cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
+    std::map<std::pair<int, int>, LaunchShape> shapes;  // (arith, order bound) -> launch shape
+    int *d_woff = nullptr, *d_hoff = nullptr;            // table offsets (shared by all arithmetics)
 };
 
 namespace {
@@ -149,6 +153,13 @@ int ensure_tables(sfmm_context *c, Arith a)
     DevTables &t = c->tab[(int)a];
     if (t.ready) return SFMM_OK;
     cudaError_t e;
+    if (!c->d_woff) {
+        if ((e = cudaMalloc(&c->d_woff, sizeof(int) * c->P)) != cudaSuccess ||
+            (e = cudaMalloc(&c->d_hoff, sizeof(int) * c->P)) != cudaSuccess ||
+            (e = cudaMemcpy(c->d_woff, c->host.woff.data(), sizeof(int) * c->P, cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMemcpy(c->d_hoff, c->host.hoff.data(), sizeof(int) * c->P, cudaMemcpyHostToDevice)) != cudaSuccess)
+            return cuda_fail(c, e, "table upload");
+    }
     if ((e = upload(&t.W, c->host.W, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
     if ((e = upload(&t.ein_M, c->host.e_in_M, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
     if ((e = upload(&t.ein_L, c->host.e_in_L, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
@@ -193,7 +204,10 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     int st = ensure_tables(c, a);
     if (st) return st;
     if (Pbound < 1) Pbound = 1;
-    LaunchShape s = translate_shape(a, Pbound);
+    auto key = std::make_pair((int)a, Pbound);
+    auto it = c->shapes.find(key);
+    if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound)).first;
+    LaunchShape s = it->second;
     if (s.acc == 0) return fail(c, SFMM_UNSUPPORTED, "order %d exceeds the GPU kernels' limit %d", Pbound, kMaxKernelOrder);
     const DevTables &t = c->tab[(int)a];
     KParams p{};
@@ -216,6 +230,8 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.perm = perm;
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
     p.W = t.W;
+    p.woff = c->d_woff;
+    p.hoff = c->d_hoff;
     p.ein = (op == SFMM_L2L) ? t.ein_L : t.ein_M;
     p.eout = (op == SFMM_M2M) ? t.eout_M : t.eout_L;
     p.H = t.H[op];
@@ -234,24 +250,47 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
 
 namespace sfmm {
 
-LaunchShape translate_shape(Arith a, int P)
+LaunchShape translate_shape(Arith a, int P, int G, int ts)
 {
     LaunchShape s;
-    if (P < 1 || P > kMaxKernelOrder) return s;
-    int acc = (P + 3) / 4;
-    acc = acc <= 2 ? 2 : (acc <= 4 ? 4 : (acc <= 6 ? 6 : 8));
+    const int per_warp = 32 / G;  // translations per warp
+    if (P < 1 || P > kMaxKernelOrder || ts < per_warp || ts % per_warp || G * ts > 256) return s;
+    int acc = (P + G - 1) / G;
+    if (G == 4) acc = acc <= 2 ? 2 : (acc <= 4 ? 4 : (acc <= 6 ? 6 : 8));
+    s.G = G;
     s.acc = acc;
-    int scap = P * (P + 1);
+    int scap = P * (P + 1) + 4;  // room for the swap loops' zero-coefficient reads past the last row
+    // element stride padded to 4 (mod 32): the G threads of the translations
+    // sharing a shared-memory phase hit distinct banks
     s.spad = scap + ((4 - scap) % 32 + 32) % 32;
-    size_t per = (size_t)s.spad * esize(a) + 5 * sizeof(uint32_t);
-    const size_t budget = 232448;
-    int ts = (int)std::min<size_t>(64, budget / per);
-    ts = (ts / 8) * 8;
-    if (ts < 8) return LaunchShape{};
     s.TS = ts;
-    s.threads = 4 * ts;
+    s.threads = G * ts;
     s.smem = (size_t)ts * s.spad * esize(a) + 5 * sizeof(uint32_t) * ts;
+    if (s.smem > 232448) return LaunchShape{};
     return s;
+}
+
+// The tile size that keeps the most threads resident per SM (shared memory
+// and registers permitting); ties go to the larger tile.  The group size
+// defaults to 4 threads per translation (SFMM_GROUP=8 selects 8).
+LaunchShape best_shape(Arith a, int P)
+{
+    static const int G = [] {
+        const char *e = std::getenv("SFMM_GROUP");
+        return (e && std::atoi(e) == 8) ? 8 : 4;
+    }();
+    LaunchShape best;
+    long best_threads = 0;
+    for (int ts = 256 / G; ts >= 32 / G; ts -= 32 / G) {
+        LaunchShape s = translate_shape(a, P, G, ts);
+        if (!s.acc) continue;
+        long th = (long)translate_blocks_per_sm(a, s) * s.threads;
+        if (th > best_threads) {
+            best_threads = th;
+            best = s;
+        }
+    }
+    return best;
 }
 
 cudaError_t launch_translate_64(const KParams &, const LaunchShape &, int, cudaStream_t);
@@ -344,6 +383,8 @@ void sfmm_destroy(sfmm_context *c)
     }
     c->d_work.release();
     if (c->d_status) cudaFree(c->d_status);
+    if (c->d_woff) cudaFree(c->d_woff);
+    if (c->d_hoff) cudaFree(c->d_hoff);
     c->h_src.release();
     c->h_dst.release();
     c->h_meta.release();

@@ -1,6 +1,7 @@
 // Explicit instantiation of the fused translation kernel for one arithmetic
 // type; included by sfmm_k64.cu, sfmm_k32.cu and sfmm_kff.cu (one translation
-// unit each, compiled in parallel).
+// unit each, compiled in parallel).  Instances: group size G in {4, 8} and
+// accumulator blocks ACC = ceil(P / G) rounded up to an instantiated size.
 #pragma once
 
 #include "sfmm_launch.hpp"
@@ -8,11 +9,11 @@
 
 namespace sfmm {
 
-template <class A, int ACC>
-static cudaError_t launch_acc(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
+template <class A, int G, int ACC>
+static cudaError_t launch_inst(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
     static bool attr_set = false;
-    auto kern = k_translate<A, ACC, false>;
+    auto kern = k_translate<A, G, ACC>;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
         if (e != cudaSuccess) return e;
@@ -22,38 +23,37 @@ static cudaError_t launch_acc(const KParams &p, const LaunchShape &s, int grid, 
     return cudaGetLastError();
 }
 
-template <class A, int ACC>
-static int occupancy_acc(const LaunchShape &s)
+template <class A, int G, int ACC>
+static int occupancy_inst(const LaunchShape &s)
 {
-    auto kern = k_translate<A, ACC, false>;
+    auto kern = k_translate<A, G, ACC>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, s.threads, s.smem) != cudaSuccess) return 1;
-    return nb > 0 ? nb : 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, s.threads, s.smem) != cudaSuccess) return 0;
+    return nb;
 }
+
+#define SFMM_FOR_SHAPES(X) \
+    X(4, 2) X(4, 4) X(4, 6) X(4, 8) X(8, 1) X(8, 2) X(8, 3) X(8, 4)
 
 template <class A>
 static cudaError_t launch_typed(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
-    switch (s.acc) {
-    case 2: return launch_acc<A, 2>(p, s, grid, st);
-    case 4: return launch_acc<A, 4>(p, s, grid, st);
-    case 6: return launch_acc<A, 6>(p, s, grid, st);
-    case 8: return launch_acc<A, 8>(p, s, grid, st);
-    default: return cudaErrorInvalidValue;
-    }
+#define X(G_, A_) \
+    if (s.G == G_ && s.acc == A_) return launch_inst<A, G_, A_>(p, s, grid, st);
+    SFMM_FOR_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
 }
 
 template <class A>
 static int occupancy_typed(const LaunchShape &s)
 {
-    switch (s.acc) {
-    case 2: return occupancy_acc<A, 2>(s);
-    case 4: return occupancy_acc<A, 4>(s);
-    case 6: return occupancy_acc<A, 6>(s);
-    case 8: return occupancy_acc<A, 8>(s);
-    default: return 1;
-    }
+#define X(G_, A_) \
+    if (s.G == G_ && s.acc == A_) return occupancy_inst<A, G_, A_>(s);
+    SFMM_FOR_SHAPES(X)
+#undef X
+    return 0;
 }
 
 }  // namespace sfmm

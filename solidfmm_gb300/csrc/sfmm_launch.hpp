@@ -17,14 +17,16 @@ enum class Arith { F64 = 0, F32 = 1, FF = 2 };
 constexpr int kMaxKernelOrder = 32;
 
 struct LaunchShape {
-    int acc = 0;       // accumulators per thread, ceil(P/4) rounded to an instantiated size
+    int G = 4;         // threads per translation
+    int acc = 0;       // accumulator blocks per thread, ceil(P/G) rounded to an instantiated size
     int TS = 0;        // translations per CTA
     int spad = 0;      // buffer elements per translation
     size_t smem = 0;   // dynamic shared memory bytes
-    int threads = 0;   // 4 * TS
+    int threads = 0;   // G * TS
 };
 
-LaunchShape translate_shape(Arith a, int P);
+LaunchShape translate_shape(Arith a, int P, int G, int ts);
+LaunchShape best_shape(Arith a, int P);
 
 // Launch the fused translation kernel (defined in sfmm_k{64,32,ff}.cu).
 cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, int grid, cudaStream_t st);

@@ -25,7 +25,9 @@ struct KParams {
     const double *shift;
     const uint32_t *perm;
     int atomic;
-    const void *W;      // arith-typed swap matrices
+    const void *W;      // arith-typed swap matrices (padded, see sfmm_tables.hpp)
+    const int *woff;    // offset of degree n's W blocks
+    const int *hoff;    // offset of column m's z matrix
     const void *ein;    // arith-typed forward edge factors (op dependent)
     const void *eout;   // arith-typed backward edge factors (op dependent)
     const void *H;      // arith-typed z matrices of this op

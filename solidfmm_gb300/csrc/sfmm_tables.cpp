@@ -64,8 +64,8 @@ HostTables build_tables(int P)
     t.woff.resize(P);
     size_t tot = 0;
     for (int n = 0; n < P; ++n) {
-        t.woff[n] = tot;
-        tot += 2 * size_t(n + 1) * (n + 1);
+        t.woff[n] = (int)tot;
+        tot += 2 * size_t(wcols(n + 1)) * wrows(n + 1);
     }
     t.W.assign(tot, 0.0);
     for (int n = 0; n < P; ++n) {
@@ -73,8 +73,9 @@ HostTables build_tables(int P)
         auto Bv = [&](int m, int l) { return B[n][(m + n) + (l + n) * w]; };
         auto D = [&](int m) { return sf(n - m) * sf(n + m); };
         auto E = [&](int m) { return m == 0 ? D(0) / s2 : D(m); };
+        const int R = wrows(d);
         double *WR = &t.W[t.woff[n]];
-        double *WI = WR + size_t(d) * d;
+        double *WI = WR + size_t(wcols(d)) * R;
         for (int i = 0; i < d; ++i)       // output row (coefficient m = i)
             for (int j = 0; j < d; ++j) { // input column (coefficient l = j)
                 // the reference's real/imag combinations (operator_data.cpp:99-147)
@@ -86,8 +87,8 @@ HostTables build_tables(int P)
                 else imf = Bv(j, i) - Bv(-j, i);
                 // keep only the checkerboard the reference stores
                 bool rnz = ((i + j + n) & 1) == 0;
-                WR[size_t(j) * d + i] = rnz ? rf * (E(i) / E(j)) : 0.0;
-                WI[size_t(j) * d + i] = (!rnz && i > 0 && j > 0) ? imf * (D(i) / D(j)) : 0.0;
+                WR[size_t(j) * R + i] = rnz ? rf * (E(i) / E(j)) : 0.0;
+                WI[size_t(j) * R + i] = (!rnz && i > 0 && j > 0) ? imf * (D(i) / D(j)) : 0.0;
             }
     }
 
@@ -110,15 +111,15 @@ HostTables build_tables(int P)
     t.hoff.resize(P);
     size_t th = 0;
     for (int m = 0; m < P; ++m) {
-        t.hoff[m] = th;
-        th += size_t(P - m) * (P - m);
+        t.hoff[m] = (int)th;
+        th += size_t(P - m + 2) * hrows(P - m);
     }
     for (int op = 0; op < 3; ++op) t.H[op].assign(th, 0.0);
     for (int m = 0; m < P; ++m) {
-        const int L = P - m;
+        const int HR = hrows(P - m);
         for (int k = m; k < P; ++k)
             for (int np = m; np < P; ++np) {
-                size_t idx = t.hoff[m] + size_t(k - m) * L + (np - m);
+                size_t idx = t.hoff[m] + size_t(k - m) * HR + (np - m);
                 double Dk = sf(k - m) * sf(k + m);
                 double Dn = sf(np - m) * sf(np + m);
                 // M2L: (-1)^(n'+m) (n'+k)! / (D^(n') D^(k))   (zm2l, translations.cpp:283-296)

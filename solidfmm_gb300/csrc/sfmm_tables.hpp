@@ -24,24 +24,31 @@ namespace sfmm {
 
 struct HostTables {
     int P = 0;
-    // W for degree n: R block at woff[n], I block at woff[n] + d*d, both
-    // column-major: entry (row i, column j) at j*d + i, d = n+1.
+    // W for degree n (d = n+1): R block at woff[n], I block at woff[n] +
+    // wcols(d)*wrows(d), both column-major: entry (row i, column j) at
+    // j*wrows(d) + i.  Rows are padded to a multiple of 8 and columns to d+3
+    // with zeros, so the kernels load coefficients without bounds checks.
     std::vector<double> W;
-    std::vector<size_t> woff;
+    std::vector<int> woff;
     // Edge factors indexed n(n+1)/2 + m:
     std::vector<double> e_in_M;   // E^(n)_m        forward of M2M/M2L inputs
     std::vector<double> e_in_L;   // 1 / F^(n)_m    forward of L2L inputs
     std::vector<double> e_out_L;  // F^(n)_m        backward of M2L/L2L outputs
     std::vector<double> e_out_M;  // 1 / E^(n)_m    backward of M2M outputs
     // z-translation matrices per op (0 M2M, 1 M2L, 2 L2L) and column m:
-    // entry (output n', input k) at hoff[m] + (k-m)*(P-m) + (n'-m).
+    // entry (output n', input k) at hoff[m] + (k-m)*hrows(P-m) + (n'-m),
+    // output rows padded with zeros to a multiple of 8.
     std::vector<double> H[3];
-    std::vector<size_t> hoff;
+    std::vector<int> hoff;
 };
 
 // Dehnen's swap matrix B_n^{m,l} (swap_matrix.cpp:149-171), all n < P,
 // stored per n as (2n+1)^2 with (m,l) at (m+n) + (l+n)(2n+1).
 std::vector<std::vector<double>> swap_matrices(int P);
+
+inline int wrows(int d) { return (d + 7) & ~7; }
+inline int wcols(int d) { return d + 3; }
+inline int hrows(int L) { return (L + 7) & ~7; }
 
 HostTables build_tables(int P);
 

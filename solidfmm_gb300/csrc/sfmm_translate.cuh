@@ -1,9 +1,8 @@
 // Fused translation kernel: M2M, M2L and L2L over a batch of translations.
 //
 // One CTA processes tiles of TS translations; each translation is handled by
-// G = 4 threads ("quad") that share its working expansion in a per-CTA
-// buffer (shared memory, or a global scratch slice when the order is too
-// large for shared memory).  Per tile:
+// a group of G threads that share its working expansion in a per-CTA
+// shared-memory buffer.  Per tile:
 //
 //   1. cooperative, coalesced gather of the TS source expansions into the
 //      buffer (solid2buf, microkernel_generic.cpp:341-359),
@@ -18,14 +17,17 @@
 //      microkernel_generic.cpp:362-380), with FP64/FP32 atomics when
 //      targets may repeat.
 //
-// Thread q of a quad owns rows i = q + 4a (a < ACC) of every degree-n swap,
-// rotation element m = q + 4a, and outputs n' = m + q + 4a of every
-// z-translation column, so each stage keeps ACC accumulators in registers and
-// reads its inputs from the buffer (quad members synchronise with
-// __syncwarp).  Loop bounds are warp-uniform maxima over the warp's eight
-// translations, exactly like the reference's lanes padded with zero orders
-// (translations.cpp:504-514); inputs past a translation's own order read as
-// zero and outputs past it are dropped.
+// Thread q of a group owns rows i = q + G a of every degree-n swap,
+// rotation elements m = q + G a, and outputs n' = m + q + G a of every
+// z-translation column; each stage keeps its accumulators in registers and
+// reads its inputs from the buffer (group members synchronise with
+// __syncwarp).  The number of accumulator blocks a stage needs,
+// ceil(d / G), is warp-uniform and selects a stage instance compiled for
+// exactly that many blocks, so no block is issued only to be predicated off.
+// Loop bounds are warp-uniform maxima over the warp's 32/G translations,
+// like the reference's lanes padded with zero orders (translations.cpp:504-514);
+// inputs past a translation's own order read as zero and outputs past it are
+// dropped.
 #pragma once
 
 #include <cstdint>
@@ -44,9 +46,6 @@ struct src_of<float> {
     using type = float;
 };
 
-__device__ __forceinline__ long long woff_of(int n) { return (long long)n * (n + 1) * (2 * n + 1) / 3; }
-__device__ __forceinline__ long long sq_sum(long long x) { return x * (x + 1) * (2 * x + 1) / 6; }
-__device__ __forceinline__ long long hoff_of(int P, int m) { return sq_sum(P) - sq_sum(P - m); }
 
 // complex helpers in FP64 for the per-translation geometry
 struct cd {
@@ -54,34 +53,277 @@ struct cd {
 };
 __device__ __forceinline__ cd cmul(cd a, cd b) { return cd{a.c * b.c - a.s * b.s, a.s * b.c + a.c * b.s}; }
 
-template <class A, int ACC, bool GBUF>
+template <int N>
+struct ic {
+    static constexpr int value = N;
+};
+
+// Calls f(ic<na>) for na in 1..MAXN (warp-uniform switch).
+template <int MAXN, class F>
+__device__ __forceinline__ void dispatch(int na, F &&f)
+{
+    switch (na) {
+    case 1: f(ic<1>{}); break;
+    case 2: if constexpr (MAXN >= 2) f(ic<2>{}); break;
+    case 3: if constexpr (MAXN >= 3) f(ic<3>{}); break;
+    case 4: if constexpr (MAXN >= 4) f(ic<4>{}); break;
+    case 5: if constexpr (MAXN >= 5) f(ic<5>{}); break;
+    case 6: if constexpr (MAXN >= 6) f(ic<6>{}); break;
+    case 7: if constexpr (MAXN >= 7) f(ic<7>{}); break;
+    case 8: if constexpr (MAXN >= 8) f(ic<8>{}); break;
+    default: break;
+    }
+}
+
+// Both swap parts of one degree: rows i = q + G a (a < NA) of W_R applied to
+// the real parts (columns j = jr, jr+2, ...) and of W_I to the imaginary
+// parts (the complementary checkerboard, columns ji = jr^1, ji+2, ...).
+// The coefficient blocks are zero-padded (rows to a multiple of 8, columns
+// to d+3) and the buffer slots past each expansion are zero, so every load is
+// unconditional; operands of the next column pair are fetched before the
+// current pair's multiply-adds (software pipelining), and the real and
+// imaginary chains are independent (2*NA accumulations per iteration).
+template <class AR, int G, int NA>
+__device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ WR, const typename AR::T *__restrict__ WI,
+                                          int R, const typename AR::Stor *xre, const typename AR::Stor *xim, int d,
+                                          int n, int q, typename AR::Acc (&ar)[NA], typename AR::Acc (&ai)[NA])
+{
+    using T = typename AR::T;
+    const int jr0 = (q + n) & 1, ji0 = jr0 ^ 1;
+    const int cnt = (d + 1) >> 1;  // iterations of the longer part
+    const T *wr_p = WR + jr0 * R + q;
+    const T *wi_p = WI + ji0 * R + q;
+    const typename AR::Stor *xr_p = xre + jr0;
+    const typename AR::Stor *xi_p = xim + ji0;
+    T xrn = AR::ld(xr_p), xin = AR::ld(xi_p);
+    T wrn[NA], win[NA];
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        wrn[a] = AR::ldt(wr_p + G * a);
+        win[a] = AR::ldt(wi_p + G * a);
+    }
+#pragma unroll 2
+    for (int t = 0; t < cnt; ++t) {
+        const T xr = xrn, xi = xin;
+        T wr[NA], wi[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            wr[a] = wrn[a];
+            wi[a] = win[a];
+        }
+        xr_p += 2;
+        xi_p += 2;
+        wr_p += 2 * R;
+        wi_p += 2 * R;
+        xrn = AR::ld(xr_p);
+        xin = AR::ld(xi_p);
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            wrn[a] = AR::ldt(wr_p + G * a);
+            win[a] = AR::ldt(wi_p + G * a);
+        }
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            AR::mac(ar[a], wr[a], xr);
+            AR::mac(ai[a], wi[a], xi);
+        }
+    }
+}
+
+// Per-thread geometry of one translation: e^{i m alpha} and e^{i m beta} for
+// the rotation elements m = q + G a this thread owns.
+template <class AR, int ACC>
+struct Trig {
+    typename AR::T ca[ACC], sa[ACC], cb[ACC], sb[ACC];
+};
+
+// One degree of the forward transform, NA = ceil(d / G) blocks.
+template <class AR, int G, int NA, int ACC>
+__device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, const typename AR::T *__restrict__ WR,
+                                               const typename AR::T *__restrict__ ein, typename AR::T f, int q,
+                                               const Trig<AR, ACC> &tg)
+{
+    using T = typename AR::T;
+    using Acc = typename AR::Acc;
+    using S = typename AR::Stor;
+    const int d = n + 1;
+    S *bre = b + n * (n + 1);
+    S *bim = b + (n + 1) * (n + 1);
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        const int m = q + G * a;
+        if (m < d) {
+            const T xr = AR::ld(bre + m);
+            const T xi = AR::ld(bim + m);
+            const T g = AR::mul(f, AR::ldt(ein + m));
+            const T gc = AR::mul(g, tg.ca[a]), gs = AR::mul(g, tg.sa[a]);
+            AR::st(bre + m, AR::dot2(gc, xr, AR::neg(gs), xi));
+            AR::st(bim + m, AR::dot2(gs, xr, gc, xi));
+        }
+    }
+    __syncwarp();
+    const int R = (d + 7) & ~7;
+    const T *WI = WR + (d + 3) * R;
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        Acc ar[NA], ai[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            ar[a] = AR::acc0();
+            ai[a] = AR::acc0();
+        }
+        swap_both<AR, G, NA>(WR, WI, R, bre, bim, d, n, q, ar, ai);
+        __syncwarp();
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            const int ii = q + G * a;
+            if (ii < d) {
+                T vr = AR::fin(ar[a]);
+                T vi = AR::fin(ai[a]);
+                if (pass == 0) {  // rotation by e^{+i m beta} between the two swaps
+                    const T wr = AR::dot2(tg.cb[a], vr, AR::neg(tg.sb[a]), vi);
+                    const T wi = AR::dot2(tg.sb[a], vr, tg.cb[a], vi);
+                    vr = wr;
+                    vi = wi;
+                }
+                AR::st(bre + ii, vr);
+                AR::st(bim + ii, vi);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// One degree of the backward transform, NA = ceil(d / G) blocks.
+template <class AR, int G, int NA, int ACC>
+__device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, const typename AR::T *__restrict__ WR,
+                                                const typename AR::T *__restrict__ eout, typename AR::T f, int q,
+                                                const Trig<AR, ACC> &tg)
+{
+    using T = typename AR::T;
+    using Acc = typename AR::Acc;
+    using S = typename AR::Stor;
+    const int d = n + 1;
+    S *bre = b + n * (n + 1);
+    S *bim = b + (n + 1) * (n + 1);
+    const int R = (d + 7) & ~7;
+    const T *WI = WR + (d + 3) * R;
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        Acc ar[NA], ai[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            ar[a] = AR::acc0();
+            ai[a] = AR::acc0();
+        }
+        swap_both<AR, G, NA>(WR, WI, R, bre, bim, d, n, q, ar, ai);
+        __syncwarp();
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            const int ii = q + G * a;
+            if (ii < d) {
+                T vr = AR::fin(ar[a]);
+                T vi = AR::fin(ai[a]);
+                if (pass == 0) {  // e^{-i m beta}
+                    const T wr = AR::dot2(tg.cb[a], vr, tg.sb[a], vi);
+                    const T wi = AR::dot2(tg.cb[a], vi, AR::neg(tg.sb[a]), vr);
+                    vr = wr;
+                    vi = wi;
+                } else {  // e^{-i m alpha}, back to the solid basis, r-power scale
+                    const T g = AR::mul(f, AR::ldt(eout + ii));
+                    const T gc = AR::mul(g, tg.ca[a]), gs = AR::mul(g, tg.sa[a]);
+                    const T wr = AR::dot2(gc, vr, gs, vi);
+                    const T wi = AR::dot2(gc, vi, AR::neg(gs), vr);
+                    vr = wr;
+                    vi = wi;
+                }
+                AR::st(bre + ii, vr);
+                AR::st(bim + ii, vi);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// One z-translation column m, outputs n' = m + q + G a (a < NA), kept where
+// n' < nout: out(n',m) = sum_{k=kbeg}^{kend-1} H_m[k-m][n'-m] in(k,m), in
+// place.  H_m's output rows are zero-padded to a multiple of 8 (HR), so the
+// coefficient loads need no bounds check.
+template <class AR, int G, int NA>
+__device__ __forceinline__ void z_column(typename AR::Stor *b, const typename AR::T *__restrict__ Hm, int HR, int m,
+                                         int kbeg, int kend, int nout, int q)
+{
+    using T = typename AR::T;
+    using Acc = typename AR::Acc;
+    Acc ar[NA], ai[NA];
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        ar[a] = AR::acc0();
+        ai[a] = AR::acc0();
+    }
+    if (kbeg < kend) {
+        int k = kbeg;
+        const T *h_p = Hm + (long long)(k - m) * HR + q;
+        T xrn = AR::ld(b + k * (k + 1) + m);
+        T xin = AR::ld(b + (k + 1) * (k + 1) + m);
+        T hn[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) hn[a] = AR::ldt(h_p + G * a);
+#pragma unroll 2
+        for (; k < kend; ++k) {
+            const T xr = xrn, xi = xin;
+            T hc[NA];
+#pragma unroll
+            for (int a = 0; a < NA; ++a) hc[a] = hn[a];
+            const int kn = min(k + 1, kend - 1);  // the last prefetch reloads column kend-1
+            h_p = Hm + (long long)(kn - m) * HR + q;
+            xrn = AR::ld(b + kn * (kn + 1) + m);
+            xin = AR::ld(b + (kn + 1) * (kn + 1) + m);
+#pragma unroll
+            for (int a = 0; a < NA; ++a) hn[a] = AR::ldt(h_p + G * a);
+#pragma unroll
+            for (int a = 0; a < NA; ++a) {
+                AR::mac(ar[a], hc[a], xr);
+                AR::mac(ai[a], hc[a], xi);
+            }
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        const int np = m + q + G * a;
+        if (np < nout) {
+            AR::st(b + np * (np + 1) + m, AR::fin(ar[a]));
+            AR::st(b + (np + 1) * (np + 1) + m, AR::fin(ai[a]));
+        }
+    }
+    __syncwarp();
+}
+
+template <class A, int G, int ACC>
 __global__ void __launch_bounds__(256) k_translate(KParams p)
 {
     using AR = arith<A>;
     using T = typename AR::T;
     using S = typename AR::Stor;
-    using Acc = typename AR::Acc;
     using Src = typename src_of<A>::type;
     static_assert(sizeof(S) == sizeof(Src), "buffer slots hold one source value");
+    static_assert(32 % G == 0, "a translation's threads must share a warp");
 
     extern __shared__ __align__(16) unsigned char smem[];
     const int TS = p.TS;
     const int tid = threadIdx.x;
-    const int q = tid & 3;
-    const int slot = tid >> 2;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int q = tid % G;
+    const int slot = tid / G;
     const int P = p.P;
     const int Scap = P * (P + 1);
     const unsigned FULL = 0xffffffffu;
 
-    S *buf0;
-    uint32_t *meta;
-    if (GBUF) {
-        buf0 = reinterpret_cast<S *>(p.scratch) + (long long)blockIdx.x * TS * p.spad;
-        meta = reinterpret_cast<uint32_t *>(smem);
-    } else {
-        buf0 = reinterpret_cast<S *>(smem);
-        meta = reinterpret_cast<uint32_t *>(smem + (size_t)TS * p.spad * sizeof(S));
-    }
+    S *buf0 = reinterpret_cast<S *>(smem);
+    uint32_t *meta = reinterpret_cast<uint32_t *>(smem + (size_t)TS * p.spad * sizeof(S));
     uint32_t *m_sidx = meta;
     uint32_t *m_tidx = meta + TS;
     uint32_t *m_pin = meta + 2 * TS;
@@ -128,7 +370,7 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         }
         const bool ident = valid && op != OP_M2L && (x * x + y * y + z * z) == 0.0;
         int ident_p = 0;
-        if (ident) {
+        if (ident) {  // zero shift: direct prefix add (translations.cpp:540-547)
             ident_p = min(pin, pout);
             pin = 0;
             pout = 0;
@@ -146,14 +388,16 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         }
         __syncthreads();
 
-        // 1. gather sources into the buffer, zero past each source's order
-        for (int e = tid; e < TS * Scap; e += blockDim.x) {
-            int s = e / Scap;
-            int c = e - s * Scap;
-            int ps = (int)m_pin[s];
-            Src v = 0;
-            if (c < ps * (ps + 1)) v = src[(long long)m_sidx[s] * p.sstride + c];
-            *reinterpret_cast<Src *>(buf0 + (long long)s * p.spad + c) = v;
+        // 1. gather sources into the buffer (one warp per expansion, lanes over
+        //    coefficients) in the arithmetic's storage format, zero past each
+        //    source's order and in the padding (the swap loops read a few
+        //    slots past a row and multiply them by zero coefficients)
+        for (int s = warp; s < TS; s += nwarps) {
+            const int ps = (int)m_pin[s];
+            const int cnt = ps * (ps + 1);
+            const Src *sp = src + (long long)m_sidx[s] * p.sstride;
+            S *bp = buf0 + (long long)s * p.spad;
+            for (int c = lane; c < p.spad; c += 32) AR::st(bp + c, c < cnt ? AR::from_d((double)sp[c]) : AR::zero());
         }
         __syncthreads();
 
@@ -167,229 +411,102 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         const double rinv = 1.0 / r;
         const cd ea = (rxy == 0) ? cd{1.0, 0.0} : cd{y / rxy, x / rxy};
         const cd eb = cd{z * rinv, -rxy * rinv};
-        T ca[ACC], sa[ACC], cb[ACC], sb[ACC];
+        Trig<AR, ACC> tg;
         {
-            cd pa{1.0, 0.0}, pb{1.0, 0.0};
-            for (int k = 0; k < q; ++k) {
-                pa = cmul(pa, ea);
-                pb = cmul(pb, eb);
+            // e^{i q gamma} by binary powers, then steps of e^{i G gamma}
+            cd pa{1.0, 0.0}, pb{1.0, 0.0}, ka = ea, kb = eb;
+            for (int bit = 1; bit < G; bit <<= 1) {
+                if (q & bit) {
+                    pa = cmul(pa, ka);
+                    pb = cmul(pb, kb);
+                }
+                ka = cmul(ka, ka);
+                kb = cmul(kb, kb);
             }
-            cd a4 = cmul(cmul(ea, ea), cmul(ea, ea));
-            cd b4 = cmul(cmul(eb, eb), cmul(eb, eb));
 #pragma unroll
             for (int a = 0; a < ACC; ++a) {
-                ca[a] = AR::from_d(pa.c);
-                sa[a] = AR::from_d(pa.s);
-                cb[a] = AR::from_d(pb.c);
-                sb[a] = AR::from_d(pb.s);
-                pa = cmul(pa, a4);
-                pb = cmul(pb, b4);
+                tg.ca[a] = AR::from_d(pa.c);
+                tg.sa[a] = AR::from_d(pa.s);
+                tg.cb[a] = AR::from_d(pb.c);
+                tg.sb[a] = AR::from_d(pb.s);
+                if (a + 1 < ACC) {
+                    pa = cmul(pa, ka);
+                    pb = cmul(pb, kb);
+                }
             }
         }
 
         // 2. forward transforms, degree by degree
         const bool Lin = (op == OP_L2L);
-        double rp = Lin ? 1.0 : rinv;          // r^n (L input) or r^-(n+1) (M input)
-        const double rstep = Lin ? r : rinv;
+        // r-power scale of degree n: r^n (L input) or r^-(n+1) (M input).
+        // Float-float steps by repeated multiplication (FP32 pipe, error
+        // ~n 2^-48); FP64 and FP32 take every power from the FP64 product.
+        constexpr bool kFF = AR::split;
+        double rp = Lin ? 1.0 : rinv;
+        const double rpstep = Lin ? r : rinv;
+        T f = AR::from_d(rp);
+        const T rstep = AR::from_d(rpstep);
         for (int n = 0; n < pin_w; ++n) {
-            const int d = n + 1;
-            S *bre = b + n * (n + 1);
-            S *bim = b + (n + 1) * (n + 1);
-            const T f = AR::from_d(rp);
+            if (!kFF) f = AR::from_d(rp);
             const T *ein = EIN + n * (n + 1) / 2;
-#pragma unroll
-            for (int a = 0; a < ACC; ++a) {
-                const int m = q + 4 * a;
-                if (m < d) {
-                    T xr = AR::from_d((double)*reinterpret_cast<const Src *>(bre + m));
-                    T xi = AR::from_d((double)*reinterpret_cast<const Src *>(bim + m));
-                    T g = AR::mul(f, AR::ldt(ein + m));
-                    T ur = AR::mul(g, AR::sub(AR::mul(ca[a], xr), AR::mul(sa[a], xi)));
-                    T ui = AR::mul(g, AR::add(AR::mul(sa[a], xr), AR::mul(ca[a], xi)));
-                    AR::st(bre + m, ur);
-                    AR::st(bim + m, ui);
-                }
-            }
-            __syncwarp();
-            const T *WR = W + woff_of(n);
-            const T *WI = WR + d * d;
-#pragma unroll 1
-            for (int pass = 0; pass < 2; ++pass) {
-                Acc ar[ACC], ai[ACC];
-#pragma unroll
-                for (int a = 0; a < ACC; ++a) {
-                    ar[a] = AR::acc0();
-                    ai[a] = AR::acc0();
-                }
-                for (int j = (q + n) & 1; j < d; j += 2) {
-                    const T xv = AR::ld(bre + j);
-#pragma unroll
-                    for (int a = 0; a < ACC; ++a) {
-                        const int ii = q + 4 * a;
-                        if (ii < d) AR::mac(ar[a], AR::ldt(WR + j * d + ii), xv);
-                    }
-                }
-                for (int j = (q + n + 1) & 1; j < d; j += 2) {
-                    const T xv = AR::ld(bim + j);
-#pragma unroll
-                    for (int a = 0; a < ACC; ++a) {
-                        const int ii = q + 4 * a;
-                        if (ii < d) AR::mac(ai[a], AR::ldt(WI + j * d + ii), xv);
-                    }
-                }
-                __syncwarp();
-#pragma unroll
-                for (int a = 0; a < ACC; ++a) {
-                    const int ii = q + 4 * a;
-                    if (ii < d) {
-                        T vr = AR::fin(ar[a]);
-                        T vi = AR::fin(ai[a]);
-                        if (pass == 0) {  // rotation by e^{+i m beta} between the two swaps
-                            T wr = AR::sub(AR::mul(cb[a], vr), AR::mul(sb[a], vi));
-                            T wi = AR::add(AR::mul(sb[a], vr), AR::mul(cb[a], vi));
-                            vr = wr;
-                            vi = wi;
-                        }
-                        AR::st(bre + ii, vr);
-                        AR::st(bim + ii, vi);
-                    }
-                }
-                __syncwarp();
-            }
-            rp *= rstep;
+            const T *WR = W + __ldg(p.woff + n);
+            dispatch<ACC>((n + G) / G, [&](auto na) {
+                forward_degree<AR, G, decltype(na)::value, ACC>(b, n, WR, ein, f, q, tg);
+            });
+            if (kFF) f = AR::mul(f, rstep);
+            rp *= rpstep;
         }
 
-        // 3. z-translation, column by column
+        // 3. z-translation, column by column.  Columns m >= min(P_in, P_out)
+        //    of the outputs stay zero (trans2swap_buf, microkernel_generic.cpp:308-338):
+        //    their rows beyond P_in were zero-filled by the gather.
         const int nout_w = pout_w;
         const int mend = min(pin_w, pout_w);
-        const T *Hop = H;
         for (int m = 0; m < mend; ++m) {
-            const int L = p.Ptab - m;
-            const T *Hm = Hop + hoff_of(p.Ptab, m);
-            Acc ar[ACC], ai[ACC];
-#pragma unroll
-            for (int a = 0; a < ACC; ++a) {
-                ar[a] = AR::acc0();
-                ai[a] = AR::acc0();
-            }
-            int kbeg = m, kend = pin_w;
-            for (int k = kbeg; k < kend; ++k) {
-                const T xr = AR::ld(b + k * (k + 1) + m);
-                const T xi = AR::ld(b + (k + 1) * (k + 1) + m);
-                const T *Hk = Hm + (long long)(k - m) * L;
-#pragma unroll
-                for (int a = 0; a < ACC; ++a) {
-                    const int np = m + q + 4 * a;
-                    if (np < nout_w) {
-                        const T h = AR::ldt(Hk + (np - m));
-                        AR::mac(ar[a], h, xr);
-                        AR::mac(ai[a], h, xi);
-                    }
-                }
-            }
-            __syncwarp();
-#pragma unroll
-            for (int a = 0; a < ACC; ++a) {
-                const int np = m + q + 4 * a;
-                if (np < nout_w) {
-                    AR::st(b + np * (np + 1) + m, AR::fin(ar[a]));
-                    AR::st(b + (np + 1) * (np + 1) + m, AR::fin(ai[a]));
-                }
-            }
-            __syncwarp();
+            const int HR = (p.Ptab - m + 7) & ~7;
+            const T *Hm = H + __ldg(p.hoff + m);
+            // M2M only needs inputs k <= n' and L2L only k >= n'
+            const int kbeg = (op == OP_L2L) ? m + q : m;
+            const int kend = (op == OP_M2M) ? min(pin_w, nout_w) : pin_w;
+            dispatch<ACC>((nout_w - m + G - 1) / G, [&](auto na) {
+                z_column<AR, G, decltype(na)::value>(b, Hm, HR, m, kbeg, kend, nout_w, q);
+            });
         }
-        // columns m >= min(P_in, P_out) of the outputs are zero (trans2swap_buf,
-        // microkernel_generic.cpp:308-338); rows below P_in may still hold inputs
-        for (int np = 0; np < nout_w; ++np) {
-#pragma unroll
-            for (int a = 0; a < ACC; ++a) {
-                const int m = q + 4 * a;
-                if (m >= mend && m <= np) {
-                    AR::st(b + np * (np + 1) + m, AR::zero());
-                    AR::st(b + (np + 1) * (np + 1) + m, AR::zero());
-                }
-            }
-        }
-        __syncwarp();
 
         // 4. backward transforms
         const bool Mout = (op == OP_M2M);
-        double rq = Mout ? r : 1.0;            // r^(n+1) (M output) or r^-n (L output)
-        const double qstep = Mout ? r : rinv;
+        double rq = Mout ? r : 1.0;  // r^(n+1) (M output) or r^-n (L output)
+        const double rqstep = Mout ? r : rinv;
+        T fo = AR::from_d(rq);
+        const T qstep = AR::from_d(rqstep);
         for (int n = 0; n < nout_w; ++n) {
-            const int d = n + 1;
-            S *bre = b + n * (n + 1);
-            S *bim = b + (n + 1) * (n + 1);
-            const T *WR = W + woff_of(n);
-            const T *WI = WR + d * d;
-            const T f = AR::from_d(rq);
+            if (!kFF) fo = AR::from_d(rq);
+            const T f = fo;
             const T *eo = EOUT + n * (n + 1) / 2;
-#pragma unroll 1
-            for (int pass = 0; pass < 2; ++pass) {
-                Acc ar[ACC], ai[ACC];
-#pragma unroll
-                for (int a = 0; a < ACC; ++a) {
-                    ar[a] = AR::acc0();
-                    ai[a] = AR::acc0();
-                }
-                for (int j = (q + n) & 1; j < d; j += 2) {
-                    const T xv = AR::ld(bre + j);
-#pragma unroll
-                    for (int a = 0; a < ACC; ++a) {
-                        const int ii = q + 4 * a;
-                        if (ii < d) AR::mac(ar[a], AR::ldt(WR + j * d + ii), xv);
-                    }
-                }
-                for (int j = (q + n + 1) & 1; j < d; j += 2) {
-                    const T xv = AR::ld(bim + j);
-#pragma unroll
-                    for (int a = 0; a < ACC; ++a) {
-                        const int ii = q + 4 * a;
-                        if (ii < d) AR::mac(ai[a], AR::ldt(WI + j * d + ii), xv);
-                    }
-                }
-                __syncwarp();
-#pragma unroll
-                for (int a = 0; a < ACC; ++a) {
-                    const int ii = q + 4 * a;
-                    if (ii < d) {
-                        T vr = AR::fin(ar[a]);
-                        T vi = AR::fin(ai[a]);
-                        if (pass == 0) {  // e^{-i m beta}
-                            T wr = AR::add(AR::mul(cb[a], vr), AR::mul(sb[a], vi));
-                            T wi = AR::sub(AR::mul(cb[a], vi), AR::mul(sb[a], vr));
-                            vr = wr;
-                            vi = wi;
-                        } else {  // e^{-i m alpha}, back to the solid basis, r-power scale
-                            T g = AR::mul(f, AR::ldt(eo + ii));
-                            T wr = AR::mul(g, AR::add(AR::mul(ca[a], vr), AR::mul(sa[a], vi)));
-                            T wi = AR::mul(g, AR::sub(AR::mul(ca[a], vi), AR::mul(sa[a], vr)));
-                            vr = wr;
-                            vi = wi;
-                        }
-                        AR::st(bre + ii, vr);
-                        AR::st(bim + ii, vi);
-                    }
-                }
-                __syncwarp();
-            }
-            rq *= qstep;
+            const T *WR = W + __ldg(p.woff + n);
+            dispatch<ACC>((n + G) / G, [&](auto na) {
+                backward_degree<AR, G, decltype(na)::value, ACC>(b, n, WR, eo, f, q, tg);
+            });
+            if (kFF) fo = AR::mul(fo, qstep);
+            rq *= rqstep;
         }
         __syncthreads();
 
-        // 5. accumulate into the targets
-        for (int e = tid; e < TS * Scap; e += blockDim.x) {
-            int s = e / Scap;
-            int c = e - s * Scap;
-            int po = (int)m_pout[s];
-            int pid = (int)m_id[s];
-            if (c < po * (po + 1) || c < pid * (pid + 1)) {
+        // 5. accumulate into the targets (one warp per expansion)
+        for (int s = warp; s < TS; s += nwarps) {
+            const int po = (int)m_pout[s];
+            const int pid = (int)m_id[s];
+            const int cnt = max(po * (po + 1), pid * (pid + 1));
+            if (!cnt) continue;
+            const S *bp = buf0 + (long long)s * p.spad;
+            const Src *sp = src + (long long)m_sidx[s] * p.sstride;
+            Src *dp = dst + (long long)m_tidx[s] * p.dstride;
+            for (int c = lane; c < cnt; c += 32) {
                 double v = 0;
-                if (c < po * (po + 1)) v = AR::to_d(AR::ld(buf0 + (long long)s * p.spad + c));
-                if (c < pid * (pid + 1)) v += (double)src[(long long)m_sidx[s] * p.sstride + c];
-                Src *dp = dst + (long long)m_tidx[s] * p.dstride + c;
-                if (p.atomic) atomicAdd(dp, (Src)v);
-                else *dp = (Src)((double)*dp + v);
+                if (c < po * (po + 1)) v = AR::to_d(AR::ld(bp + c));
+                if (c < pid * (pid + 1)) v += (double)sp[c];
+                if (p.atomic) atomicAdd(dp + c, (Src)v);
+                else dp[c] = (Src)((double)dp[c] + v);
             }
         }
         __syncthreads();
