@@ -63,8 +63,12 @@ typedef struct sfmm_context sfmm_context;
 /* Operator context of order P (the reference's operator_data<real>(P),
  * solidfmm/operator_data.cpp:151-244): builds the rotation/swap/z-translation
  * tables in FP64 on the host and uploads them to `device`.
- * P == 0 -> SFMM_INVALID_ARG; P > 18 (F32) or P > 86 (F64) -> SFMM_OVERFLOW
- * (the reference's limits, operator_data.cpp:37-45,157-164). */
+ * P == 0 -> SFMM_INVALID_ARG; P > 86 (F64) -> SFMM_OVERFLOW (the reference's
+ * limit, operator_data.cpp:37-45,157-164).  F32 contexts go up to P = 28
+ * (the reference's float limit is 18 because it keeps factorials in FP32;
+ * these kernels keep them in FP64 and in the orthogonal basis, so orders up
+ * to 28 stay in range); the C++ drop-in operator_data<float> keeps the
+ * reference's limit of 18. */
 int sfmm_create(sfmm_context **ctx, int dtype, size_t P, int device);
 void sfmm_destroy(sfmm_context *ctx);
 size_t sfmm_order(const sfmm_context *ctx);
@@ -144,6 +148,14 @@ int sfmm_measure_fma_peak(int fp64, int device, double *flops_per_second);
 /* Diagnostics: measured throughput of 32x32->64-bit integer multiply-adds
  * (operations/s, one per multiply-add). */
 int sfmm_measure_imad_peak(int device, double *ops_per_second);
+
+/* Diagnostics: the FP64 operator tables of order P as dense row-major
+ * arrays.  which: 0/1 = W_R/W_I of degree n (d x d, entry (i,j)); 2/3/4 =
+ * z-translation matrix H_m of M2M/M2L/L2L for column m = n ((P-m) x (P-m),
+ * entry (n'-m, k-m)); 5..8 = edge factors e_in_M, e_in_L, e_out_L, e_out_M
+ * (index n(n+1)/2+m).  Writes min(cap, count) values to out (may be NULL)
+ * and the full count to *count.  Host only, needs no GPU. */
+int sfmm_host_table(size_t P, int which, int n, double *out, size_t cap, size_t *count);
 
 /* Number of kernel launches issued by this context since creation. */
 uint64_t sfmm_launch_count(const sfmm_context *ctx);

@@ -26,6 +26,7 @@ EXPORTS = [
     "sfmm_create", "sfmm_destroy", "sfmm_order", "sfmm_data_type", "sfmm_last_error", "sfmm_status_string",
     "sfmm_set_stream", "sfmm_translate_device", "sfmm_device_status", "sfmm_translate_host_packed",
     "sfmm_translate_host", "sfmm_bucket_by_order", "sfmm_p2x_device", "sfmm_launch_count",
+    "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak",
 ]
 
 
@@ -73,8 +74,36 @@ def load():
     L.sfmm_p2x_device.argtypes = [vp, C.c_int, sz, sz, dp, dp, dp, vp, sz]
     L.sfmm_launch_count.argtypes = [vp]
     L.sfmm_launch_count.restype = C.c_uint64
+    L.sfmm_host_table.argtypes = [sz, C.c_int, C.c_int, vp, sz, C.POINTER(C.c_size_t)]
+    L.sfmm_measure_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.sfmm_measure_imad_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     _lib = L
     return L
+
+
+def host_table(P: int, which: int, n: int = 0) -> np.ndarray:
+    """FP64 operator table (see sfmm_host_table in include/sfmm.h); host only."""
+    L = load()
+    cnt = C.c_size_t(0)
+    rc = L.sfmm_host_table(P, which, n, None, 0, C.byref(cnt))
+    if rc:
+        raise SfmmError(rc, "sfmm_host_table")
+    out = np.zeros(cnt.value)
+    L.sfmm_host_table(P, which, n, out.ctypes.data, cnt.value, C.byref(cnt))
+    return out
+
+
+def measure_peak(kind: str, device: int = 0) -> float:
+    """Measured pipe throughput: 'fp64' / 'fp32' (flop/s) or 'imad' (int64 MAC/s)."""
+    L = load()
+    v = C.c_double(0)
+    if kind == "imad":
+        rc = L.sfmm_measure_imad_peak(device, C.byref(v))
+    else:
+        rc = L.sfmm_measure_fma_peak(1 if kind == "fp64" else 0, device, C.byref(v))
+    if rc:
+        raise SfmmError(rc, "peak probe")
+    return v.value
 
 
 def _ptr(x):

@@ -209,6 +209,8 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound)).first;
     LaunchShape s = it->second;
     if (s.acc == 0) return fail(c, SFMM_UNSUPPORTED, "order %d exceeds the GPU kernels' limit %d", Pbound, kMaxKernelOrder);
+    if (a != Arith::F64 && Pbound > kMaxFloatOrder)
+        return fail(c, SFMM_UNSUPPORTED, "order %d exceeds %d, the limit of FP32-range arithmetic", Pbound, kMaxFloatOrder);
     const DevTables &t = c->tab[(int)a];
     KParams p{};
     p.op = op;
@@ -232,6 +234,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.W = t.W;
     p.woff = c->d_woff;
     p.hoff = c->d_hoff;
+    p.rowpad = c->host.pad;
     p.ein = (op == SFMM_L2L) ? t.ein_L : t.ein_M;
     p.eout = (op == SFMM_M2M) ? t.eout_M : t.eout_L;
     p.H = t.H[op];
@@ -255,8 +258,10 @@ LaunchShape translate_shape(Arith a, int P, int G, int ts)
     LaunchShape s;
     const int per_warp = 32 / G;  // translations per warp
     if (P < 1 || P > kMaxKernelOrder || ts < per_warp || ts % per_warp || G * ts > 256) return s;
+    if ((G == 32) != (P > 32)) return s;  // one warp per translation exactly for orders above 32
     int acc = (P + G - 1) / G;
     if (G == 4) acc = acc <= 2 ? 2 : (acc <= 4 ? 4 : (acc <= 6 ? 6 : 8));
+    if (G == 32) acc = acc <= 2 ? 2 : 3;
     s.G = G;
     s.acc = acc;
     int scap = P * (P + 1) + 4;  // room for the swap loops' zero-coefficient reads past the last row
@@ -275,10 +280,11 @@ LaunchShape translate_shape(Arith a, int P, int G, int ts)
 // defaults to 4 threads per translation (SFMM_GROUP=8 selects 8).
 LaunchShape best_shape(Arith a, int P)
 {
-    static const int G = [] {
+    static const int Gsmall = [] {
         const char *e = std::getenv("SFMM_GROUP");
         return (e && std::atoi(e) == 8) ? 8 : 4;
     }();
+    const int G = P > 32 ? 32 : Gsmall;
     LaunchShape best;
     long best_threads = 0;
     for (int ts = 256 / G; ts >= 32 / G; ts -= 32 / G) {
@@ -343,7 +349,7 @@ int sfmm_create(sfmm_context **out, int dtype, size_t P, int device)
     *out = nullptr;
     if (dtype != SFMM_F32 && dtype != SFMM_F64) return SFMM_INVALID_ARG;
     if (P == 0) return SFMM_INVALID_ARG;
-    if ((dtype == SFMM_F32 && P > 18) || (dtype == SFMM_F64 && P > 86)) return SFMM_OVERFLOW;
+    if ((dtype == SFMM_F32 && P > (size_t)kMaxFloatOrder) || (dtype == SFMM_F64 && P > 86)) return SFMM_OVERFLOW;
     sfmm_context *c = new (std::nothrow) sfmm_context;
     if (!c) return SFMM_OOM;
     c->dtype = dtype;
@@ -396,6 +402,39 @@ size_t sfmm_order(const sfmm_context *c) { return c ? (size_t)c->P : 0; }
 int sfmm_data_type(const sfmm_context *c) { return c ? c->dtype : -1; }
 const char *sfmm_last_error(const sfmm_context *c) { return c ? c->err.c_str() : "null context"; }
 uint64_t sfmm_launch_count(const sfmm_context *c) { return c ? c->launches : 0; }
+
+int sfmm_host_table(size_t P, int which, int n, double *out, size_t cap, size_t *count)
+{
+    if (P == 0 || P > 86 || !count) return SFMM_INVALID_ARG;
+    HostTables t;
+    try {
+        t = build_tables((int)P);
+    } catch (const std::bad_alloc &) {
+        return SFMM_OOM;
+    }
+    std::vector<double> v;
+    if (which == 0 || which == 1) {  // dense W_R / W_I of degree n, row-major (i, j)
+        if (n < 0 || n >= (int)P) return SFMM_INVALID_ARG;
+        const int d = n + 1, R = wrows(d, t.pad);
+        const double *blk = &t.W[t.woff[n]] + (which == 1 ? (size_t)wcols(d) * R : 0);
+        for (int i = 0; i < d; ++i)
+            for (int j = 0; j < d; ++j) v.push_back(blk[(size_t)j * R + i]);
+    } else if (which >= 2 && which <= 4) {  // dense H_m (n', k) of op which-2, row-major, m = n
+        const int m = n, L = (int)P - m;
+        if (m < 0 || m >= (int)P) return SFMM_INVALID_ARG;
+        const int HR = hrows(L, t.pad);
+        for (int a = 0; a < L; ++a)
+            for (int k = 0; k < L; ++k) v.push_back(t.H[which - 2][t.hoff[m] + (size_t)k * HR + a]);
+    } else if (which >= 5 && which <= 8) {  // edge factors
+        const std::vector<double> *e[] = {&t.e_in_M, &t.e_in_L, &t.e_out_L, &t.e_out_M};
+        v = *e[which - 5];
+    } else {
+        return SFMM_INVALID_ARG;
+    }
+    *count = v.size();
+    if (out) std::memcpy(out, v.data(), sizeof(double) * std::min(cap, v.size()));
+    return SFMM_OK;
+}
 
 int sfmm_set_stream(sfmm_context *c, void *stream)
 {

@@ -1,6 +1,6 @@
 // Explicit instantiation of the fused translation kernel for one arithmetic
 // type; included by sfmm_k64.cu, sfmm_k32.cu and sfmm_kff.cu (one translation
-// unit each, compiled in parallel).  Instances: group size G in {4, 8} and
+// unit each, compiled in parallel).  Instances: group size G in {4, 8, 32} and
 // accumulator blocks ACC = ceil(P / G) rounded up to an instantiated size.
 #pragma once
 
@@ -34,7 +34,7 @@ static int occupancy_inst(const LaunchShape &s)
 }
 
 #define SFMM_FOR_SHAPES(X) \
-    X(4, 2) X(4, 4) X(4, 6) X(4, 8) X(8, 1) X(8, 2) X(8, 3) X(8, 4)
+    X(4, 2) X(4, 4) X(4, 6) X(4, 8) X(8, 1) X(8, 2) X(8, 3) X(8, 4) X(32, 2) X(32, 3)
 
 template <class A>
 static cudaError_t launch_typed(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)

@@ -12,9 +12,13 @@ struct KParams;
 
 enum class Arith { F64 = 0, F32 = 1, FF = 2 };
 
-// Largest order the fused translation kernel supports (accumulator arrays
-// are sized ceil(P/4) per thread).
-constexpr int kMaxKernelOrder = 32;
+// Largest order the fused translation kernel supports: 4 threads per
+// translation up to 32, one warp per translation up to 96 (the reference's
+// FP64 limit is 86).
+constexpr int kMaxKernelOrder = 96;
+// FP32 and float-float arithmetic keep the orthogonal-basis scale factors
+// sqrt((n-m)!(n+m)!) in FP32 range only up to this order.
+constexpr int kMaxFloatOrder = 28;
 
 struct LaunchShape {
     int G = 4;         // threads per translation

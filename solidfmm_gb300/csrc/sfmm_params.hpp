@@ -28,6 +28,7 @@ struct KParams {
     const void *W;      // arith-typed swap matrices (padded, see sfmm_tables.hpp)
     const int *woff;    // offset of degree n's W blocks
     const int *hoff;    // offset of column m's z matrix
+    int rowpad;         // row padding of W and H blocks (8 or 32)
     const void *ein;    // arith-typed forward edge factors (op dependent)
     const void *eout;   // arith-typed backward edge factors (op dependent)
     const void *H;      // arith-typed z matrices of this op

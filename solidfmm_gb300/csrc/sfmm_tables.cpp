@@ -54,6 +54,8 @@ HostTables build_tables(int P)
 {
     HostTables t;
     t.P = P;
+    const int pad = row_pad(P);
+    t.pad = pad;
     auto B = swap_matrices(P);
     SqrtFac sf(2 * P + 2);
     std::vector<double> fac(2 * P + 2);
@@ -65,7 +67,7 @@ HostTables build_tables(int P)
     size_t tot = 0;
     for (int n = 0; n < P; ++n) {
         t.woff[n] = (int)tot;
-        tot += 2 * size_t(wcols(n + 1)) * wrows(n + 1);
+        tot += 2 * size_t(wcols(n + 1)) * wrows(n + 1, pad);
     }
     t.W.assign(tot, 0.0);
     for (int n = 0; n < P; ++n) {
@@ -73,7 +75,7 @@ HostTables build_tables(int P)
         auto Bv = [&](int m, int l) { return B[n][(m + n) + (l + n) * w]; };
         auto D = [&](int m) { return sf(n - m) * sf(n + m); };
         auto E = [&](int m) { return m == 0 ? D(0) / s2 : D(m); };
-        const int R = wrows(d);
+        const int R = wrows(d, pad);
         double *WR = &t.W[t.woff[n]];
         double *WI = WR + size_t(wcols(d)) * R;
         for (int i = 0; i < d; ++i)       // output row (coefficient m = i)
@@ -112,11 +114,11 @@ HostTables build_tables(int P)
     size_t th = 0;
     for (int m = 0; m < P; ++m) {
         t.hoff[m] = (int)th;
-        th += size_t(P - m + 2) * hrows(P - m);
+        th += size_t(P - m + 2) * hrows(P - m, pad);
     }
     for (int op = 0; op < 3; ++op) t.H[op].assign(th, 0.0);
     for (int m = 0; m < P; ++m) {
-        const int HR = hrows(P - m);
+        const int HR = hrows(P - m, pad);
         for (int k = m; k < P; ++k)
             for (int np = m; np < P; ++np) {
                 size_t idx = t.hoff[m] + size_t(k - m) * HR + (np - m);

@@ -25,9 +25,11 @@ namespace sfmm {
 struct HostTables {
     int P = 0;
     // W for degree n (d = n+1): R block at woff[n], I block at woff[n] +
-    // wcols(d)*wrows(d), both column-major: entry (row i, column j) at
-    // j*wrows(d) + i.  Rows are padded to a multiple of 8 and columns to d+3
-    // with zeros, so the kernels load coefficients without bounds checks.
+    // wcols(d)*wrows(d,pad), both column-major: entry (row i, column j) at
+    // j*wrows(d,pad) + i.  Rows are padded to a multiple of row_pad(P) and
+    // columns to d+3 with zeros, so the kernels load coefficients without
+    // bounds checks.
+    int pad = 8;
     std::vector<double> W;
     std::vector<int> woff;
     // Edge factors indexed n(n+1)/2 + m:
@@ -36,8 +38,8 @@ struct HostTables {
     std::vector<double> e_out_L;  // F^(n)_m        backward of M2L/L2L outputs
     std::vector<double> e_out_M;  // 1 / E^(n)_m    backward of M2M outputs
     // z-translation matrices per op (0 M2M, 1 M2L, 2 L2L) and column m:
-    // entry (output n', input k) at hoff[m] + (k-m)*hrows(P-m) + (n'-m),
-    // output rows padded with zeros to a multiple of 8.
+    // entry (output n', input k) at hoff[m] + (k-m)*hrows(P-m,pad) + (n'-m),
+    // output rows padded with zeros to a multiple of row_pad(P).
     std::vector<double> H[3];
     std::vector<int> hoff;
 };
@@ -46,9 +48,13 @@ struct HostTables {
 // stored per n as (2n+1)^2 with (m,l) at (m+n) + (l+n)(2n+1).
 std::vector<std::vector<double>> swap_matrices(int P);
 
-inline int wrows(int d) { return (d + 7) & ~7; }
+// Row padding of the coefficient blocks: 8 when the kernels run 4 threads
+// per translation (orders up to 32), 32 when they run one warp per
+// translation (larger orders).
+inline int row_pad(int P) { return P <= 32 ? 8 : 32; }
+inline int wrows(int d, int pad) { return (d + pad - 1) & ~(pad - 1); }
 inline int wcols(int d) { return d + 3; }
-inline int hrows(int L) { return (L + 7) & ~7; }
+inline int hrows(int L, int pad) { return (L + pad - 1) & ~(pad - 1); }
 
 HostTables build_tables(int P);
 

@@ -139,7 +139,8 @@ struct Trig {
 
 // One degree of the forward transform, NA = ceil(d / G) blocks.
 template <class AR, int G, int NA, int ACC>
-__device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, const typename AR::T *__restrict__ WR,
+__device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, int rowpad,
+                                               const typename AR::T *__restrict__ WR,
                                                const typename AR::T *__restrict__ ein, typename AR::T f, int q,
                                                const Trig<AR, ACC> &tg)
 {
@@ -162,7 +163,7 @@ __device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, cons
         }
     }
     __syncwarp();
-    const int R = (d + 7) & ~7;
+    const int R = (d + rowpad - 1) & ~(rowpad - 1);
     const T *WI = WR + (d + 3) * R;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
@@ -196,7 +197,8 @@ __device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, cons
 
 // One degree of the backward transform, NA = ceil(d / G) blocks.
 template <class AR, int G, int NA, int ACC>
-__device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, const typename AR::T *__restrict__ WR,
+__device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, int rowpad,
+                                                const typename AR::T *__restrict__ WR,
                                                 const typename AR::T *__restrict__ eout, typename AR::T f, int q,
                                                 const Trig<AR, ACC> &tg)
 {
@@ -206,7 +208,7 @@ __device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, con
     const int d = n + 1;
     S *bre = b + n * (n + 1);
     S *bim = b + (n + 1) * (n + 1);
-    const int R = (d + 7) & ~7;
+    const int R = (d + rowpad - 1) & ~(rowpad - 1);
     const T *WI = WR + (d + 3) * R;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
@@ -451,7 +453,7 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             const T *ein = EIN + n * (n + 1) / 2;
             const T *WR = W + __ldg(p.woff + n);
             dispatch<ACC>((n + G) / G, [&](auto na) {
-                forward_degree<AR, G, decltype(na)::value, ACC>(b, n, WR, ein, f, q, tg);
+                forward_degree<AR, G, decltype(na)::value, ACC>(b, n, p.rowpad, WR, ein, f, q, tg);
             });
             if (kFF) f = AR::mul(f, rstep);
             rp *= rpstep;
@@ -463,7 +465,7 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         const int nout_w = pout_w;
         const int mend = min(pin_w, pout_w);
         for (int m = 0; m < mend; ++m) {
-            const int HR = (p.Ptab - m + 7) & ~7;
+            const int HR = (p.Ptab - m + p.rowpad - 1) & ~(p.rowpad - 1);
             const T *Hm = H + __ldg(p.hoff + m);
             // M2M only needs inputs k <= n' and L2L only k >= n'
             const int kbeg = (op == OP_L2L) ? m + q : m;
@@ -485,7 +487,7 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             const T *eo = EOUT + n * (n + 1) / 2;
             const T *WR = W + __ldg(p.woff + n);
             dispatch<ACC>((n + G) / G, [&](auto na) {
-                backward_degree<AR, G, decltype(na)::value, ACC>(b, n, WR, eo, f, q, tg);
+                backward_degree<AR, G, decltype(na)::value, ACC>(b, n, p.rowpad, WR, eo, f, q, tg);
             });
             if (kFF) fo = AR::mul(fo, qstep);
             rq *= rqstep;

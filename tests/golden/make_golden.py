@@ -78,6 +78,17 @@ def main():
     for k, v in cases.items():
         for f, a in v.items():
             out[f"{k}/{f}"] = a
+    # harmonics R, S, dR, dS of order 12 at a few points (harmonics.cpp:32-349)
+    pts = [(0.3, -0.2, 0.5), (1.1, 0.2, -0.9), (-0.7, 0.4, 0.1), (0.0, 0.0, 1.5)]
+    for wi, which in enumerate(("R", "S", "dR", "dS")):
+        rows = []
+        for (px, py, pz) in pts:
+            dim = 3 if which.startswith("d") else 1
+            buf = np.zeros(12 * 13 * dim)
+            O.ref().ref_harmonic_d(wi, 12, px, py, pz, buf)
+            rows.append(buf)
+        out[f"harmonics/{which}"] = np.array(rows)
+    out["harmonics/points"] = np.array(pts)
     B = {}
     for n in range(7):
         B[n] = np.array([[O.ref().ref_swap_B(n, m, l) for l in range(-n, n + 1)] for m in range(-n, n + 1)])
