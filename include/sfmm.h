@@ -133,6 +133,24 @@ int sfmm_translate_host(sfmm_context *ctx, int op, int precision, size_t n,
 int sfmm_bucket_by_order(sfmm_context *ctx, size_t n, const uint32_t *p_in, const uint32_t *p_out,
                          uint32_t *order);
 
+/* Bucketing without any allocation (no counterpart in the reference; the
+ * reference has no GPU and allocates its buffers on the host).  For callers
+ * that cannot allocate device memory -- codes that give the whole GPU to their
+ * own memory pool, processes under a hard device-memory cap, or hot paths
+ * where an allocation would stall -- and so cannot create a context either.
+ * Same result as sfmm_bucket_by_order (a permutation of 0..n-1 in `order`
+ * grouping equal (p_in, p_out) pairs; order within a group is unspecified)
+ * for orders up to max_order <= 86; larger max_order returns
+ * SFMM_ORDER_RANGE and does nothing.  Runs on the CUDA device current at the
+ * call and on `stream` (cudaStream_t as void*, NULL = default stream),
+ * asynchronously.  Its counters live in one fixed 30 KiB device array per
+ * GPU that every call shares: concurrent calls whose kernels overlap on the
+ * GPU race and must be serialised (e.g. on one stream).  The first call on a
+ * device looks up the array's device address, so make it before any stream
+ * capture.  Calls no cudaMalloc/cudaFree. */
+int sfmm_bucket_by_order_noalloc(size_t n, const uint32_t *p_in, const uint32_t *p_out, uint32_t *order,
+                                 size_t max_order, void *stream);
+
 /* P2M / P2L on the device (the reference's fmadd(q, harmonics::R/S(P, x-c), E),
  * solid.cpp:70-104 with harmonics.cpp:32-80,177-224): for expansion j,
  *   out[j] += sum_{k<nq} charge[j*nq+k] * R(pos[j*nq+k] - centre[j])   (kind 0)

@@ -26,7 +26,7 @@ EXPORTS = [
     "sfmm_create", "sfmm_destroy", "sfmm_order", "sfmm_data_type", "sfmm_last_error", "sfmm_status_string",
     "sfmm_set_stream", "sfmm_translate_device", "sfmm_device_status", "sfmm_translate_host_packed",
     "sfmm_translate_host", "sfmm_bucket_by_order", "sfmm_p2x_device", "sfmm_launch_count",
-    "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak",
+    "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak", "sfmm_bucket_by_order_noalloc",
 ]
 
 
@@ -77,6 +77,7 @@ def load():
     L.sfmm_host_table.argtypes = [sz, C.c_int, C.c_int, vp, sz, C.POINTER(C.c_size_t)]
     L.sfmm_measure_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.sfmm_measure_imad_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.sfmm_bucket_by_order_noalloc.argtypes = [sz, u32p, u32p, u32p, sz, vp]
     _lib = L
     return L
 

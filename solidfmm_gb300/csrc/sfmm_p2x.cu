@@ -10,7 +10,10 @@
 // (p_in, p_out), so that warps see uniform orders.
 #include <algorithm>
 #include <cstdint>
+#include <map>
+#include <mutex>
 
+#include "sfmm.h"
 #include "sfmm_launch.hpp"
 
 namespace sfmm {
@@ -178,3 +181,55 @@ cudaError_t launch_bucket(long long n, const uint32_t *pin, const uint32_t *pout
 }
 
 }  // namespace sfmm
+
+// ---- bucketing without allocation ----
+//
+// The counters of the bucketing sort live in a fixed device array instead of
+// context memory, for callers that must not allocate device memory at all:
+// codes that hand the whole device to their own memory pool, run under a
+// hard per-process memory cap, or issue work from paths where a cudaMalloc
+// would stall or fail.  The array is sized for orders up to 86 (the largest
+// order a solidfmm operator accepts), 87 x 87 counters = 30 KiB; every GPU
+// that loads the library keeps it until the process exits.
+
+namespace {
+
+constexpr int kStaticBucketMaxOrder = 86;
+constexpr int kStaticBucketKeys = (kStaticBucketMaxOrder + 1) * (kStaticBucketMaxOrder + 1);
+
+__device__ __align__(256) uint32_t g_bucket_counters[kStaticBucketKeys];
+
+// device address of g_bucket_counters, looked up once per device
+std::mutex g_bucket_mtx;
+std::map<int, uint32_t *> g_bucket_addr;
+
+}  // namespace
+
+extern "C" int sfmm_bucket_by_order_noalloc(size_t n, const uint32_t *p_in, const uint32_t *p_out, uint32_t *order,
+                                            size_t max_order, void *stream)
+{
+    if (max_order > (size_t)kStaticBucketMaxOrder) return SFMM_ORDER_RANGE;
+    if (n > 0xffffffffull) return SFMM_INVALID_ARG;
+    if (n == 0) return SFMM_OK;
+    if (!p_in || !p_out || !order) return SFMM_INVALID_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SFMM_CUDA_ERROR;
+    uint32_t *counters = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_bucket_mtx);
+        auto it = g_bucket_addr.find(dev);
+        if (it == g_bucket_addr.end()) {
+            // the host-side symbol is only a stand-in for the array; the
+            // kernels need its device address on this device
+            if (cudaGetSymbolAddress((void **)&counters, g_bucket_counters) != cudaSuccess) return SFMM_CUDA_ERROR;
+            g_bucket_addr.emplace(dev, counters);
+        } else {
+            counters = it->second;
+        }
+    }
+    // the counters are cleared on the stream before use (launch_bucket)
+    cudaError_t e = sfmm::launch_bucket((long long)n, p_in, p_out, order, counters, (int)max_order,
+                                        (cudaStream_t)stream);
+    return e == cudaSuccess ? SFMM_OK : SFMM_CUDA_ERROR;
+}
+
