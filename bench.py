@@ -35,6 +35,9 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # name: (op, P, N, charges per source)
     "m2l16": ("m2l", 16, 2_000_000, 64),
+    # the same kernel on 65 536 translations (1 GB of expansions, still far
+    # above L2): the case that ncu --set full captures
+    "m2l16_small": ("m2l", 16, 65_536, 64),
     "m2l10": ("m2l", 10, 100_000, 64),
     "m2l20": ("m2l", 20, 1_000_000, 128),
     "m2m20": ("m2m", 20, 1_000_000, 128),
