@@ -46,11 +46,22 @@ typedef enum { SFMM_F32 = 0, SFMM_F64 = 1 } sfmm_dtype;
 typedef enum { SFMM_M2M = 0, SFMM_M2L = 1, SFMM_L2L = 2 } sfmm_op;
 
 /* Arithmetic of the translation kernels.
- * PLAIN: the storage type's own arithmetic (FP64 for SFMM_F64, FP32 for SFMM_F32).
- * SPLIT: double-FP32 (float-float) arithmetic on the FP32 pipes for every
- *        swap, rotation and z-translation; FP64 geometry and FP64 final
- *        accumulation into the targets.  SFMM_F64 contexts only. */
-typedef enum { SFMM_PLAIN = 0, SFMM_SPLIT = 1 } sfmm_precision;
+ * PLAIN:    the storage type's own arithmetic (FP64 for SFMM_F64, FP32 for
+ *           SFMM_F32).
+ * SPLIT:    FP64 expansions in, FP64 accumulation out, the translation itself
+ *           on the FP32 and integer pipes with relative error <= 1e-7 in the
+ *           orthonormal (Schmidt) basis: swaps and polar rotations in block
+ *           fixed point (int32 mantissas with one exponent per degree row,
+ *           Q1.30 coefficients, exact int64 accumulation), the azimuthal
+ *           rotations, r-power scaling and z-translation in float-float.
+ *           M2M batches with an order bound above 18 run the SPLIT_FF
+ *           arithmetic: there the rotation method's error growth with the
+ *           degree would take 30-bit mantissas past 1e-7.
+ * SPLIT_FF: the same with float-float (double-FP32, ~2^-44 per operation)
+ *           for every stage: relative error ~1e-13 at order 16.
+ * The split modes need an SFMM_F64 context and orders <= 28 (FP32 exponent
+ * range of the orthogonal-basis scale factors). */
+typedef enum { SFMM_PLAIN = 0, SFMM_SPLIT = 1, SFMM_SPLIT_FF = 2 } sfmm_precision;
 
 /* flags for the batch calls */
 enum {
@@ -126,6 +137,18 @@ int sfmm_translate_host(sfmm_context *ctx, int op, int precision, size_t n,
                         const void *const *src, const size_t *p_in,
                         void *const *dst, const size_t *p_out, size_t dim,
                         const void *x, const void *y, const void *z);
+
+/* Launch shape.  The translation kernels run G threads per translation: 4
+ * or 8 for order bounds up to 32, one warp (32) above.  By default a context
+ * takes G per (precision, order bound) from a built-in table measured on
+ * GB300; sfmm_set_group pins G for one (precision, order bound) pair, and
+ * sfmm_tune times every supported G on n synthetic translations of `op` on
+ * the context's stream (synchronising it) and keeps the fastest.  `group`
+ * (may be NULL) receives the kept G, `rate` (may be NULL) its measured
+ * translations per second.  order_bound 0 = the context order. */
+int sfmm_set_group(sfmm_context *ctx, int precision, size_t order_bound, int group);
+int sfmm_tune(sfmm_context *ctx, int op, int precision, size_t order_bound, size_t n, int *group,
+              double *rate);
 
 /* Bucket a device batch by (p_in, p_out): writes a permutation of 0..n-1 into
  * `order` (device, n entries) so that translations of equal order pairs are

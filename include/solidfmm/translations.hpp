@@ -138,8 +138,9 @@ void l2l_unchecked(const operator_data<double> &op, threadlocal_buffer<double> &
 
 // GB300 extension (no counterpart in the reference): arithmetic of the
 // double-precision calls in this thread.  false (default) = plain FP64;
-// true = float-float swaps, rotations and z-translations with FP64 geometry
-// and FP64 accumulation (include/sfmm.h, SFMM_SPLIT).
+// true = split precision (include/sfmm.h, SFMM_SPLIT): FP64 expansions and
+// accumulation, the translation on the FP32 and integer pipes with relative
+// error <= 1e-7 in the orthonormal basis.
 void set_split_precision(bool enable) noexcept;
 bool split_precision() noexcept;
 

@@ -15,7 +15,7 @@ from . import build as _build
 
 F32, F64 = 0, 1
 M2M, M2L, L2L = 0, 1, 2
-PLAIN, SPLIT = 0, 1
+PLAIN, SPLIT, SPLIT_FF = 0, 1, 2
 TARGETS_UNIQUE, TARGETS_REPEAT = 0, 1
 OPS = {"m2m": M2M, "m2l": M2L, "l2l": L2L}
 
@@ -27,6 +27,7 @@ EXPORTS = [
     "sfmm_set_stream", "sfmm_translate_device", "sfmm_device_status", "sfmm_translate_host_packed",
     "sfmm_translate_host", "sfmm_bucket_by_order", "sfmm_p2x_device", "sfmm_launch_count",
     "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak", "sfmm_bucket_by_order_noalloc",
+    "sfmm_set_group", "sfmm_tune",
 ]
 
 
@@ -64,6 +65,8 @@ def load():
     L.sfmm_status_string.argtypes = [C.c_int]
     L.sfmm_status_string.restype = C.c_char_p
     L.sfmm_set_stream.argtypes = [vp, vp]
+    L.sfmm_set_group.argtypes = [vp, C.c_int, sz, C.c_int]
+    L.sfmm_tune.argtypes = [vp, C.c_int, C.c_int, sz, sz, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     L.sfmm_translate_device.argtypes = [vp, C.c_int, C.c_int, sz, vp, sz, sz, u32p, vp, sz, sz, u32p, u32p, u32p,
                                         dp, u32p, C.c_int, sz]
     L.sfmm_device_status.argtypes = [vp, C.POINTER(C.c_int)]
@@ -151,6 +154,18 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None):
         self._check(self.L.sfmm_set_stream(self.h, stream_ptr))
+
+    def set_group(self, precision: int, group: int, order_bound: int = 0):
+        """Pin the threads per translation for (precision, order bound)."""
+        self._check(self.L.sfmm_set_group(self.h, precision, order_bound, group))
+
+    def tune(self, op, precision: int, n: int = 65536, order_bound: int = 0):
+        """Time every supported group size on n synthetic translations and
+        keep the fastest; returns (group, translations per second)."""
+        g = C.c_int(0)
+        r = C.c_double(0)
+        self._check(self.L.sfmm_tune(self.h, OPS.get(op, op), precision, order_bound, n, C.byref(g), C.byref(r)))
+        return g.value, r.value
 
     def translate_device(self, op, precision, n, src, src_stride, src_count, dst, dst_stride, dst_count, p_in, p_out,
                          shift, src_index=None, dst_index=None, order=None, repeat=False, order_bound=0):

@@ -31,6 +31,7 @@ struct arith<double> {
     using Acc = double;
     static __device__ __forceinline__ T zero() { return 0.0; }
     static __device__ __forceinline__ T from_d(double x) { return x; }
+    static __device__ __forceinline__ T from_src(double x) { return x; }
     static __device__ __forceinline__ double to_d(T x) { return x; }
     static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
     static __device__ __forceinline__ T add(T a, T b) { return a + b; }
@@ -54,6 +55,7 @@ struct arith<float> {
     using Acc = float;
     static __device__ __forceinline__ T zero() { return 0.f; }
     static __device__ __forceinline__ T from_d(double x) { return (float)x; }
+    static __device__ __forceinline__ T from_src(float x) { return x; }
     static __device__ __forceinline__ double to_d(T x) { return (double)x; }
     static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
     static __device__ __forceinline__ T add(T a, T b) { return a + b; }
@@ -103,6 +105,70 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b)
     return ff_norm(p, e);
 }
 
+// 2^e (|e| <= 126) as a float, and x * 2^e as two exact power-of-two
+// multiplications (the first never leaves the normal range for the
+// exponents used here, so only the final product rounds).
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
+__device__ __forceinline__ float ldexp2(float x, int e)
+{
+    const int e1 = e / 2;
+    return __fmul_rn(__fmul_rn(x, pow2f(e1)), pow2f(e - e1));
+}
+
+// double -> float-float with integer and FP32 operations only (the FP64
+// pipe is 1/64 of the FP32 rate).  The 53-bit significand M splits into its
+// top 24 bits A (exact in a float) and the remaining 29 bits B (rounded to 24
+// bits); x = A 2^k + B 2^(k-29), then one Fast2Sum.  The pair represents x to
+// about 2^-48 relative; |x| < 2^-151 becomes 0 and |x| >= 2^128 overflows.
+__device__ __forceinline__ ff ff_from_d_int(double x)
+{
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    const unsigned A = 0x800000u | ((hw & 0xfffffu) << 3) | (lw >> 29);
+    const unsigned B = lw & 0x1fffffffu;
+    const int k = min(e - 1023 - 23, 106);
+    float h = ldexp2(__uint2float_rn(A), k);
+    float l = ldexp2(__uint2float_rn(B), k - 29);
+    if (e < 1023 - 151) h = l = 0.f;
+    if (hw >> 31) {
+        h = -h;
+        l = -l;
+    }
+    return ff_norm(h, l);
+}
+
+// float -> double by re-biasing the exponent (exact); zero included, other
+// non-normal values take the conversion instruction.
+__device__ __forceinline__ double d_from_f_int(float f)
+{
+    const unsigned w = __float_as_uint(f);
+    const unsigned ex = (w >> 23) & 0xffu;
+    if ((w << 1) == 0u) return __hiloint2double((int)(w & 0x80000000u), 0);
+    if (ex == 0u || ex == 0xffu) return (double)f;
+    const unsigned hi = (w & 0x80000000u) | ((ex + 896u) << 20) | ((w & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(w << 29));
+}
+
+// float-float square root and reciprocal: one Newton step from the FP32
+// result (error ~2^-44 relative).
+__device__ __forceinline__ ff ff_sqrt(ff a)
+{
+    if (!(a.hi > 0.f)) return ff{0.f, 0.f};
+    const float s = __fsqrt_rn(a.hi);
+    const float p = __fmul_rn(s, s);
+    const float pe = __fmaf_rn(s, s, -p);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), a.lo);  // a - s^2
+    return ff_norm(s, __fmul_rn(r, __fdiv_rn(0.5f, s)));
+}
+
+__device__ __forceinline__ ff ff_rcp(ff b)
+{
+    const float r = __frcp_rn(b.hi);
+    // 1 - b r, with the b.hi r product split exactly
+    const float e = __fsub_rn(__fmaf_rn(-b.hi, r, 1.f), __fmul_rn(b.lo, r));
+    return ff_norm(r, __fmul_rn(r, e));
+}
+
 // unnormalised accumulator: value = hi + lo, lo collects every rounding error
 struct ffacc {
     float hi, lo;
@@ -116,6 +182,8 @@ struct arith<ff> {
     using Acc = ffacc;
     static __device__ __forceinline__ T zero() { return ff{0.f, 0.f}; }
     static __device__ __forceinline__ T from_d(double x) { return ff_from_d(x); }
+    // source coefficients: converted without FP64 instructions
+    static __device__ __forceinline__ T from_src(double x) { return ff_from_d_int(x); }
     static __device__ __forceinline__ double to_d(T x) { return ff_to_d(x); }
     static __device__ __forceinline__ T mul(T a, T b) { return ff_mul(a, b); }
     static __device__ __forceinline__ T add(T a, T b) { return ff_add(a, b); }

@@ -30,6 +30,7 @@ namespace {
 struct DevTables {
     void *W = nullptr, *ein_M = nullptr, *ein_L = nullptr, *eout_L = nullptr, *eout_M = nullptr;
     void *H[3] = {nullptr, nullptr, nullptr};
+    void *Wq = nullptr;  // Q1.30 swap matrices (fixed-point variant only)
     bool ready = false;
 };
 
@@ -84,7 +85,7 @@ struct sfmm_context {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     HostTables host;
-    DevTables tab[3];  // indexed by Arith
+    DevTables tab[4];  // indexed by Arith
     std::string err;
     uint64_t launches = 0;
     std::mutex mtx;  // serialises host-path calls (one translator object, one stream)
@@ -167,13 +168,21 @@ int ensure_tables(sfmm_context *c, Arith a)
     if ((e = upload(&t.eout_M, c->host.e_out_M, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
     for (int k = 0; k < 3; ++k)
         if ((e = upload(&t.H[k], c->host.H[k], a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+    if (a == Arith::FFQ) {
+        // |w| <= 1 (orthogonal matrices): round(w 2^30) fits int32
+        std::vector<int32_t> q(c->host.W.size());
+        for (size_t i = 0; i < q.size(); ++i) q[i] = (int32_t)std::llround(std::ldexp(c->host.W[i], 30));
+        if ((e = cudaMalloc(&t.Wq, q.size() * sizeof(int32_t) + 16)) != cudaSuccess ||
+            (e = cudaMemcpy(t.Wq, q.data(), q.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return cuda_fail(c, e, "table upload");
+    }
     t.ready = true;
     return SFMM_OK;
 }
 
 void free_tables(DevTables &t)
 {
-    void *ps[] = {t.W, t.ein_M, t.ein_L, t.eout_L, t.eout_M, t.H[0], t.H[1], t.H[2]};
+    void *ps[] = {t.W, t.ein_M, t.ein_L, t.eout_L, t.eout_M, t.H[0], t.H[1], t.H[2], t.Wq};
     for (void *p : ps)
         if (p) cudaFree(p);
     t = DevTables{};
@@ -185,13 +194,25 @@ int arith_of(sfmm_context *c, int precision, Arith *out)
         *out = c->dtype == SFMM_F64 ? Arith::F64 : Arith::F32;
         return SFMM_OK;
     }
-    if (precision == SFMM_SPLIT) {
+    if (precision == SFMM_SPLIT || precision == SFMM_SPLIT_FF) {
         if (c->dtype != SFMM_F64)
             return fail(c, SFMM_UNSUPPORTED, "split precision needs an FP64 context (FP64 accumulation targets)");
-        *out = Arith::FF;
+        *out = precision == SFMM_SPLIT ? Arith::FFQ : Arith::FF;
         return SFMM_OK;
     }
     return fail(c, SFMM_INVALID_ARG, "unknown precision mode %d", precision);
+}
+
+// Split precision keeps its 1e-7 contract (orthonormal basis) with the
+// fixed-point rotations for M2L and L2L up to order 28 and M2M up to order
+// 18.  Past that the rotation method's own error growth with the degree
+// (about 1.35x per degree for M2M, in every arithmetic) pushes 30-bit
+// mantissas above 1e-7, and the batch runs in float-float instead.
+constexpr int kFixedM2MOrder = 18;
+Arith resolve_arith(Arith a, int op, int Pbound)
+{
+    if (a == Arith::FFQ && op == SFMM_M2M && Pbound > kFixedM2MOrder) return Arith::FF;
+    return a;
 }
 
 // The launch itself: validated arguments, device pointers.
@@ -201,12 +222,13 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
               const uint32_t *perm, int flags)
 {
     if (n == 0) return SFMM_OK;
+    a = resolve_arith(a, op, Pbound);
     int st = ensure_tables(c, a);
     if (st) return st;
     if (Pbound < 1) Pbound = 1;
     auto key = std::make_pair((int)a, Pbound);
     auto it = c->shapes.find(key);
-    if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound)).first;
+    if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound, default_group(a, Pbound))).first;
     LaunchShape s = it->second;
     if (s.acc == 0) return fail(c, SFMM_UNSUPPORTED, "order %d exceeds the GPU kernels' limit %d", Pbound, kMaxKernelOrder);
     if (a != Arith::F64 && Pbound > kMaxFloatOrder)
@@ -232,6 +254,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.perm = perm;
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
     p.W = t.W;
+    p.Wq = static_cast<const int *>(t.Wq);
     p.woff = c->d_woff;
     p.hoff = c->d_hoff;
     p.rowpad = c->host.pad;
@@ -265,9 +288,13 @@ LaunchShape translate_shape(Arith a, int P, int G, int ts)
     s.G = G;
     s.acc = acc;
     int scap = P * (P + 1) + 4;  // room for the swap loops' zero-coefficient reads past the last row
-    // element stride padded to 4 (mod 32): the G threads of the translations
-    // sharing a shared-memory phase hit distinct banks
-    s.spad = scap + ((4 - scap) % 32 + 32) % 32;
+    // Translation stride in shared memory: the translations of a warp read
+    // the same element offset at once (all threads of a group, two adjacent
+    // slots); strides of 2 (mod 16) 8-byte slots or 4 (mod 32) 4-byte slots
+    // start consecutive translations 4 banks apart, so those reads are
+    // conflict-free.
+    const int mod = esize(a) == 8 ? 16 : 32, want = esize(a) == 8 ? 2 : 4;
+    s.spad = scap + ((want - scap) % mod + mod) % mod;
     s.TS = ts;
     s.threads = G * ts;
     s.smem = (size_t)ts * s.spad * esize(a) + 5 * sizeof(uint32_t) * ts;
@@ -275,16 +302,28 @@ LaunchShape translate_shape(Arith a, int P, int G, int ts)
     return s;
 }
 
-// The tile size that keeps the most threads resident per SM (shared memory
-// and registers permitting); ties go to the larger tile.  The group size
-// defaults to 4 threads per translation (SFMM_GROUP=8 selects 8).
-LaunchShape best_shape(Arith a, int P)
+// Threads per translation by default: one warp above order 32; below, 4 or
+// 8 from a sweep on GB300 (M2L, uniform orders 2..32, both group sizes): 8
+// threads pay off once the per-translation buffers limit the SM to a few
+// warps and the group's own arithmetic is cheap enough to leave latency
+// exposed (FP64 from order 24, FP32 from 24, both split modes from 14).
+int default_group(Arith a, int P)
 {
-    static const int Gsmall = [] {
-        const char *e = std::getenv("SFMM_GROUP");
-        return (e && std::atoi(e) == 8) ? 8 : 4;
-    }();
-    const int G = P > 32 ? 32 : Gsmall;
+    if (P > 32) return 32;
+    switch (a) {
+    case Arith::F64: return P >= 24 ? 8 : 4;
+    case Arith::F32: return P >= 24 ? 8 : 4;
+    case Arith::FF: return P >= 14 ? 8 : 4;
+    case Arith::FFQ: return P >= 14 ? 8 : 4;
+    }
+    return 4;
+}
+
+// The tile size that keeps the most threads resident per SM (shared memory
+// and registers permitting) for G threads per translation; ties go to the
+// larger tile.
+LaunchShape best_shape(Arith a, int P, int G)
+{
     LaunchShape best;
     long best_threads = 0;
     for (int ts = 256 / G; ts >= 32 / G; ts -= 32 / G) {
@@ -302,15 +341,18 @@ LaunchShape best_shape(Arith a, int P)
 cudaError_t launch_translate_64(const KParams &, const LaunchShape &, int, cudaStream_t);
 cudaError_t launch_translate_32(const KParams &, const LaunchShape &, int, cudaStream_t);
 cudaError_t launch_translate_ff(const KParams &, const LaunchShape &, int, cudaStream_t);
+cudaError_t launch_translate_ffq(const KParams &, const LaunchShape &, int, cudaStream_t);
 int occupancy_64(const LaunchShape &);
 int occupancy_32(const LaunchShape &);
 int occupancy_ff(const LaunchShape &);
+int occupancy_ffq(const LaunchShape &);
 
 cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
     switch (a) {
     case Arith::F64: return launch_translate_64(p, s, grid, st);
     case Arith::F32: return launch_translate_32(p, s, grid, st);
+    case Arith::FFQ: return launch_translate_ffq(p, s, grid, st);
     default: return launch_translate_ff(p, s, grid, st);
     }
 }
@@ -320,6 +362,7 @@ int translate_blocks_per_sm(Arith a, const LaunchShape &s)
     switch (a) {
     case Arith::F64: return occupancy_64(s);
     case Arith::F32: return occupancy_32(s);
+    case Arith::FFQ: return occupancy_ffq(s);
     default: return occupancy_ff(s);
     }
 }
@@ -415,10 +458,9 @@ int sfmm_host_table(size_t P, int which, int n, double *out, size_t cap, size_t 
     std::vector<double> v;
     if (which == 0 || which == 1) {  // dense W_R / W_I of degree n, row-major (i, j)
         if (n < 0 || n >= (int)P) return SFMM_INVALID_ARG;
-        const int d = n + 1, R = wrows(d, t.pad);
-        const double *blk = &t.W[t.woff[n]] + (which == 1 ? (size_t)wcols(d) * R : 0);
+        const int d = n + 1;
         for (int i = 0; i < d; ++i)
-            for (int j = 0; j < d; ++j) v.push_back(blk[(size_t)j * R + i]);
+            for (int j = 0; j < d; ++j) v.push_back(w_entry(t, n, which, i, j));
     } else if (which >= 2 && which <= 4) {  // dense H_m (n', k) of op which-2, row-major, m = n
         const int m = n, L = (int)P - m;
         if (m < 0 || m >= (int)P) return SFMM_INVALID_ARG;
@@ -440,6 +482,112 @@ int sfmm_set_stream(sfmm_context *c, void *stream)
 {
     if (!c) return SFMM_INVALID_ARG;
     c->stream = (cudaStream_t)stream;
+    return SFMM_OK;
+}
+
+int sfmm_set_group(sfmm_context *c, int precision, size_t order_bound, int group)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mtx);
+    Arith a;
+    int st = arith_of(c, precision, &a);
+    if (st) return st;
+    if (order_bound > (size_t)c->P) return fail(c, SFMM_ORDER_RANGE, "order bound %zu exceeds the context order %d", order_bound, c->P);
+    const int Pb = order_bound ? (int)order_bound : c->P;
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, SFMM_CUDA_ERROR, "cannot select device %d", c->device);
+    LaunchShape s = best_shape(a, Pb, group);
+    if (!s.acc) return fail(c, SFMM_INVALID_ARG, "no kernel runs %d threads per translation at order %d", group, Pb);
+    c->shapes[std::make_pair((int)a, Pb)] = s;
+    return SFMM_OK;
+}
+
+int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t n, int *group, double *rate)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mtx);
+    if (op < SFMM_M2M || op > SFMM_L2L) return fail(c, SFMM_INVALID_ARG, "unknown operation %d", op);
+    Arith a;
+    int st = arith_of(c, precision, &a);
+    if (st) return st;
+    if (order_bound > (size_t)c->P) return fail(c, SFMM_ORDER_RANGE, "order bound %zu exceeds the context order %d", order_bound, c->P);
+    if (n == 0 || n > (size_t)1 << 24) return fail(c, SFMM_INVALID_ARG, "tuning sample of %zu translations", n);
+    const int Pb = order_bound ? (int)order_bound : c->P;
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, SFMM_CUDA_ERROR, "cannot select device %d", c->device);
+    const size_t S = (size_t)Pb * (Pb + 1), es = c->dtype == SFMM_F64 ? 8 : 4;
+    // synthetic batch: constant coefficients, orders Pb, shifts of length
+    // 2.5 in varied directions (the kernels' cost does not depend on values)
+    std::vector<uint32_t> ord(n, (uint32_t)Pb);
+    std::vector<double> sh(3 * n);
+    for (size_t i = 0; i < n; ++i) {
+        const double t = 0.7 * (double)i, u = 0.3 + 2.4 * (double)(i % 97) / 97.0;
+        sh[3 * i] = 2.5 * std::sin(u) * std::cos(t);
+        sh[3 * i + 1] = 2.5 * std::sin(u) * std::sin(t);
+        sh[3 * i + 2] = 2.5 * std::cos(u);
+    }
+    void *src = nullptr, *dst = nullptr, *meta = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&] {
+        if (src) cudaFree(src);
+        if (dst) cudaFree(dst);
+        if (meta) cudaFree(meta);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&src, n * S * es)) != cudaSuccess || (e = cudaMalloc(&dst, n * S * es)) != cudaSuccess ||
+        (e = cudaMalloc(&meta, n * (2 * sizeof(uint32_t) + 3 * sizeof(double)))) != cudaSuccess) {
+        cleanup();
+        return e == cudaErrorMemoryAllocation ? fail(c, SFMM_OOM, "tuning buffers") : cuda_fail(c, e, "tuning buffers");
+    }
+    double *d_shift = static_cast<double *>(meta);
+    uint32_t *d_ord = reinterpret_cast<uint32_t *>(d_shift + 3 * n);
+    cudaStream_t stream = c->stream;
+    if ((e = cudaMemsetAsync(src, 0x3e, n * S * es, stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(dst, 0, n * S * es, stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_shift, sh.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice, stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_ord, ord.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream)) != cudaSuccess ||
+        (e = cudaEventCreate(&e0)) != cudaSuccess || (e = cudaEventCreate(&e1)) != cudaSuccess) {
+        cleanup();
+        return cuda_fail(c, e, "tuning setup");
+    }
+    a = resolve_arith(a, op, Pb);
+    const auto key = std::make_pair((int)a, Pb);
+    LaunchShape best;
+    double best_rate = 0;
+    const int groups[] = {4, 8, 32};
+    for (int G : groups) {
+        LaunchShape s = best_shape(a, Pb, G);
+        if (!s.acc) continue;
+        c->shapes[key] = s;
+        float ms = 0;
+        for (int rep = 0; rep < 2 && st == SFMM_OK; ++rep) {  // warm-up, then timed
+            if (rep == 1 && (e = cudaEventRecord(e0, stream)) != cudaSuccess) break;
+            for (int k = 0; k < (rep ? 3 : 1) && st == SFMM_OK; ++k)
+                st = run_batch(c, stream, op, a, Pb, (long long)n, src, (long long)S, (long long)n, nullptr, dst,
+                               (long long)S, (long long)n, nullptr, d_ord, d_ord, d_shift, nullptr, 0);
+            if (rep == 1 && (e = cudaEventRecord(e1, stream)) != cudaSuccess) break;
+        }
+        if (st == SFMM_OK && e == cudaSuccess && (e = cudaEventSynchronize(e1)) == cudaSuccess)
+            e = cudaEventElapsedTime(&ms, e0, e1);
+        if (st != SFMM_OK || e != cudaSuccess) {
+            c->shapes.erase(key);
+            cleanup();
+            return st != SFMM_OK ? st : cuda_fail(c, e, "tuning run");
+        }
+        const double r = ms > 0 ? 3.0 * (double)n / (ms * 1e-3) : 0.0;
+        if (r > best_rate) {
+            best_rate = r;
+            best = s;
+        }
+    }
+    cleanup();
+    if (!best.acc) {
+        c->shapes.erase(key);
+        return fail(c, SFMM_UNSUPPORTED, "no kernel for order %d", Pb);
+    }
+    c->shapes[key] = best;
+    if (group) *group = best.G;
+    if (rate) *rate = best_rate;
     return SFMM_OK;
 }
 

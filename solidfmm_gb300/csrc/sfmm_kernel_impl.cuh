@@ -1,7 +1,9 @@
 // Explicit instantiation of the fused translation kernel for one arithmetic
-// type; included by sfmm_k64.cu, sfmm_k32.cu and sfmm_kff.cu (one translation
-// unit each, compiled in parallel).  Instances: group size G in {4, 8, 32} and
-// accumulator blocks ACC = ceil(P / G) rounded up to an instantiated size.
+// type; included by sfmm_k64.cu, sfmm_k32.cu, sfmm_kff.cu and sfmm_kffq.cu
+// (one translation unit each, compiled in parallel).  Instances: group size G
+// in {4, 8, 32} and accumulator blocks ACC = ceil(P / G) rounded up to an
+// instantiated size; the fixed-point float-float variant (orders <= 28) has
+// no one-warp-per-translation instances.
 #pragma once
 
 #include "sfmm_launch.hpp"
@@ -9,11 +11,11 @@
 
 namespace sfmm {
 
-template <class A, int G, int ACC>
+template <class A, int G, int ACC, bool FIX>
 static cudaError_t launch_inst(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
     static bool attr_set = false;
-    auto kern = k_translate<A, G, ACC>;
+    auto kern = k_translate<A, G, ACC, FIX>;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
         if (e != cudaSuccess) return e;
@@ -23,10 +25,10 @@ static cudaError_t launch_inst(const KParams &p, const LaunchShape &s, int grid,
     return cudaGetLastError();
 }
 
-template <class A, int G, int ACC>
+template <class A, int G, int ACC, bool FIX>
 static int occupancy_inst(const LaunchShape &s)
 {
-    auto kern = k_translate<A, G, ACC>;
+    auto kern = k_translate<A, G, ACC, FIX>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, s.threads, s.smem) != cudaSuccess) return 0;
@@ -36,21 +38,23 @@ static int occupancy_inst(const LaunchShape &s)
 #define SFMM_FOR_SHAPES(X) \
     X(4, 2) X(4, 4) X(4, 6) X(4, 8) X(8, 1) X(8, 2) X(8, 3) X(8, 4) X(32, 2) X(32, 3)
 
-template <class A>
+template <class A, bool FIX = false>
 static cudaError_t launch_typed(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
 #define X(G_, A_) \
-    if (s.G == G_ && s.acc == A_) return launch_inst<A, G_, A_>(p, s, grid, st);
+    if constexpr (!(FIX && G_ == 32))                                   \
+        if (s.G == G_ && s.acc == A_) return launch_inst<A, G_, A_, FIX>(p, s, grid, st);
     SFMM_FOR_SHAPES(X)
 #undef X
     return cudaErrorInvalidValue;
 }
 
-template <class A>
+template <class A, bool FIX = false>
 static int occupancy_typed(const LaunchShape &s)
 {
 #define X(G_, A_) \
-    if (s.G == G_ && s.acc == A_) return occupancy_inst<A, G_, A_>(s);
+    if constexpr (!(FIX && G_ == 32))              \
+        if (s.G == G_ && s.acc == A_) return occupancy_inst<A, G_, A_, FIX>(s);
     SFMM_FOR_SHAPES(X)
 #undef X
     return 0;

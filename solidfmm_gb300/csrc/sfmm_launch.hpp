@@ -10,7 +10,8 @@ namespace sfmm {
 
 struct KParams;
 
-enum class Arith { F64 = 0, F32 = 1, FF = 2 };
+// FFQ: float-float with block fixed-point swaps and beta rotations
+enum class Arith { F64 = 0, F32 = 1, FF = 2, FFQ = 3 };
 
 // Largest order the fused translation kernel supports: 4 threads per
 // translation up to 32, one warp per translation up to 96 (the reference's
@@ -30,9 +31,10 @@ struct LaunchShape {
 };
 
 LaunchShape translate_shape(Arith a, int P, int G, int ts);
-LaunchShape best_shape(Arith a, int P);
+int default_group(Arith a, int P);
+LaunchShape best_shape(Arith a, int P, int G);
 
-// Launch the fused translation kernel (defined in sfmm_k{64,32,ff}.cu).
+// Launch the fused translation kernel (defined in sfmm_k{64,32,ff,ffq}.cu).
 cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, int grid, cudaStream_t st);
 int translate_blocks_per_sm(Arith a, const LaunchShape &s);
 

@@ -26,6 +26,7 @@ struct KParams {
     const uint32_t *perm;
     int atomic;
     const void *W;      // arith-typed swap matrices (padded, see sfmm_tables.hpp)
+    const int *Wq;      // swap matrices in Q1.30 (fixed-point variant), same layout as W
     const int *woff;    // offset of degree n's W blocks
     const int *hoff;    // offset of column m's z matrix
     int rowpad;         // row padding of W and H blocks (8 or 32)

@@ -50,6 +50,15 @@ struct SqrtFac {
 
 }  // namespace
 
+double w_entry(const HostTables &t, int n, int part, int i, int j)
+{
+    const int d = n + 1, R = wrows(d, t.pad);
+    if (i < 0 || j < 0 || i >= d || j >= d) return 0.0;
+    const bool rnz = ((i + j + n) & 1) == 0;
+    if (rnz != (part == 0)) return 0.0;
+    return t.W[t.woff[n] + (part ? size_t(wcols(d)) * R : 0) + size_t(j >> 1) * R + i];
+}
+
 HostTables build_tables(int P)
 {
     HostTables t;
@@ -88,9 +97,10 @@ HostTables build_tables(int P)
                 if (j & 1) imf = Bv(j, i) + Bv(-j, i);
                 else imf = Bv(j, i) - Bv(-j, i);
                 // keep only the checkerboard the reference stores
-                bool rnz = ((i + j + n) & 1) == 0;
-                WR[size_t(j) * R + i] = rnz ? rf * (E(i) / E(j)) : 0.0;
-                WI[size_t(j) * R + i] = (!rnz && i > 0 && j > 0) ? imf * (D(i) / D(j)) : 0.0;
+                const bool rnz = ((i + j + n) & 1) == 0;
+                const size_t slot = size_t(j >> 1) * R + i;  // j = jr(i) + 2t or ji(i) + 2t
+                if (rnz) WR[slot] = rf * (E(i) / E(j));
+                else if (i > 0 && j > 0) WI[slot] = imf * (D(i) / D(j));
             }
     }
 

@@ -25,10 +25,13 @@ namespace sfmm {
 struct HostTables {
     int P = 0;
     // W for degree n (d = n+1): R block at woff[n], I block at woff[n] +
-    // wcols(d)*wrows(d,pad), both column-major: entry (row i, column j) at
-    // j*wrows(d,pad) + i.  Rows are padded to a multiple of row_pad(P) and
-    // columns to d+3 with zeros, so the kernels load coefficients without
-    // bounds checks.
+    // wcols(d)*wrows(d,pad).  Only the checkerboard a swap uses is stored:
+    // W_R(i, j) is nonzero only for j = jr(i) + 2t with jr(i) = (i+n) & 1,
+    // W_I(i, j) only for j = ji(i) + 2t with ji(i) = jr(i) ^ 1; slot t of row
+    // i sits at t*wrows(d,pad) + i.  Rows are padded to a multiple of
+    // row_pad(P) and slots to wcols(d) = (d+3)/2 with zeros (the swap loops
+    // prefetch one slot past the last column), so the kernels load
+    // coefficients without bounds checks.
     int pad = 8;
     std::vector<double> W;
     std::vector<int> woff;
@@ -53,7 +56,10 @@ std::vector<std::vector<double>> swap_matrices(int P);
 // translation (larger orders).
 inline int row_pad(int P) { return P <= 32 ? 8 : 32; }
 inline int wrows(int d, int pad) { return (d + pad - 1) & ~(pad - 1); }
-inline int wcols(int d) { return d + 3; }
+inline int wcols(int d) { return (d + 3) / 2; }
+// W_R (part 0) or W_I (part 1) of degree n at (row i, column j), from the
+// compact layout
+double w_entry(const HostTables &t, int n, int part, int i, int j);
 inline int hrows(int L, int pad) { return (L + pad - 1) & ~(pad - 1); }
 
 HostTables build_tables(int P);

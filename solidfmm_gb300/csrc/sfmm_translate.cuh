@@ -33,6 +33,7 @@
 #include <cstdint>
 
 #include "sfmm_arith.cuh"
+#include "sfmm_fixed.cuh"
 #include "sfmm_params.hpp"
 
 namespace sfmm {
@@ -78,9 +79,10 @@ __device__ __forceinline__ void dispatch(int na, F &&f)
 // Both swap parts of one degree: rows i = q + G a (a < NA) of W_R applied to
 // the real parts (columns j = jr, jr+2, ...) and of W_I to the imaginary
 // parts (the complementary checkerboard, columns ji = jr^1, ji+2, ...).
-// The coefficient blocks are zero-padded (rows to a multiple of 8, columns
-// to d+3) and the buffer slots past each expansion are zero, so every load is
-// unconditional; operands of the next column pair are fetched before the
+// The coefficient blocks hold only that checkerboard (slot t of row i is
+// column jr(i) + 2t), zero-padded (rows to a multiple of 8, slots to
+// (d+3)/2), and the buffer slots past each expansion are zero, so every load
+// is unconditional; operands of the next column pair are fetched before the
 // current pair's multiply-adds (software pipelining), and the real and
 // imaginary chains are independent (2*NA accumulations per iteration).
 template <class AR, int G, int NA>
@@ -91,8 +93,8 @@ __device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ WR,
     using T = typename AR::T;
     const int jr0 = (q + n) & 1, ji0 = jr0 ^ 1;
     const int cnt = (d + 1) >> 1;  // iterations of the longer part
-    const T *wr_p = WR + jr0 * R + q;
-    const T *wi_p = WI + ji0 * R + q;
+    const T *wr_p = WR + q;
+    const T *wi_p = WI + q;
     const typename AR::Stor *xr_p = xre + jr0;
     const typename AR::Stor *xi_p = xim + ji0;
     T xrn = AR::ld(xr_p), xin = AR::ld(xi_p);
@@ -113,8 +115,8 @@ __device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ WR,
         }
         xr_p += 2;
         xi_p += 2;
-        wr_p += 2 * R;
-        wi_p += 2 * R;
+        wr_p += R;
+        wi_p += R;
         xrn = AR::ld(xr_p);
         xin = AR::ld(xi_p);
 #pragma unroll
@@ -164,7 +166,7 @@ __device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, int 
     }
     __syncwarp();
     const int R = (d + rowpad - 1) & ~(rowpad - 1);
-    const T *WI = WR + (d + 3) * R;
+    const T *WI = WR + ((d + 3) >> 1) * R;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         Acc ar[NA], ai[NA];
@@ -209,7 +211,7 @@ __device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, int
     S *bre = b + n * (n + 1);
     S *bim = b + (n + 1) * (n + 1);
     const int R = (d + rowpad - 1) & ~(rowpad - 1);
-    const T *WI = WR + (d + 3) * R;
+    const T *WI = WR + ((d + 3) >> 1) * R;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         Acc ar[NA], ai[NA];
@@ -241,6 +243,161 @@ __device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, int
                 }
                 AR::st(bre + ii, vr);
                 AR::st(bim + ii, vi);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Q1.30 cos / sin of m beta for the rotation elements a thread owns
+template <int ACC>
+struct FixTrig {
+    int c[ACC], s[ACC];
+};
+
+__device__ __forceinline__ void st_fixed(float2 *p, int v) { *reinterpret_cast<int *>(p) = v; }
+
+// One degree of the forward transform with the swaps and the beta rotation
+// in block fixed point: float-float edge, conversion at the row's block
+// exponent, integer swap, renormalise, integer rotation, integer swap,
+// renormalise, back to float-float.
+template <int G, int NA, int ACC>
+__device__ __forceinline__ void forward_degree_fixed(float2 *b, int n, int rowpad, const int *__restrict__ WRq,
+                                                     const ff *__restrict__ ein, ff f, int q,
+                                                     const Trig<arith<ff>, ACC> &tg, const FixTrig<ACC> &tq)
+{
+    using AR = arith<ff>;
+    const int d = n + 1;
+    float2 *bre = b + n * (n + 1);
+    float2 *bim = b + (n + 1) * (n + 1);
+    ff vr[NA], vi[NA];
+    float mx = 0.f;
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        const int m = q + G * a;
+        vr[a] = vi[a] = AR::zero();
+        if (m < d) {
+            const ff xr = AR::ld(bre + m);
+            const ff xi = AR::ld(bim + m);
+            const ff g = AR::mul(f, AR::ldt(ein + m));
+            const ff gc = AR::mul(g, tg.ca[a]), gs = AR::mul(g, tg.sa[a]);
+            vr[a] = AR::dot2(gc, xr, AR::neg(gs), xi);
+            vi[a] = AR::dot2(gs, xr, gc, xi);
+            mx = fmaxf(mx, fmaxf(fabsf(vr[a].hi), fabsf(vi[a].hi)));
+        }
+    }
+    int E = block_exponent(group_max<G>(mx));
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        const int m = q + G * a;
+        if (m < d) {
+            st_fixed(bre + m, ff_to_fixed(vr[a], E));
+            st_fixed(bim + m, ff_to_fixed(vi[a], E));
+        }
+    }
+    __syncwarp();
+    const int R = (d + rowpad - 1) & ~(rowpad - 1);
+    const int *WIq = WRq + ((d + 3) >> 1) * R;
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        long long ar[NA], ai[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) ar[a] = ai[a] = 0;
+        swap_both_fixed<G, NA>(WRq, WIq, R, bre, bim, d, n, q, ar, ai);
+        unsigned long long am = 0;
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            const unsigned long long ur = (unsigned long long)llabs(ar[a]), ui = (unsigned long long)llabs(ai[a]);
+            am = ur > am ? ur : am;
+            am = ui > am ? ui : am;
+        }
+        const int sh = renorm_shift(group_max<G>(am), kFixBits);
+        E += sh - 30;
+        __syncwarp();
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            const int ii = q + G * a;
+            if (ii < d) {
+                const int xr = round_shift(ar[a], sh), xi = round_shift(ai[a], sh);
+                if (pass == 0) {  // rotation by e^{+i m beta} between the two swaps
+                    st_fixed(bre + ii, rot_q30(tq.c[a], xr, tq.s[a], xi));
+                    st_fixed(bim + ii, rot_q30(tq.c[a], xi, -tq.s[a], xr));
+                } else {
+                    AR::st(bre + ii, fixed_to_ff(xr, E));
+                    AR::st(bim + ii, fixed_to_ff(xi, E));
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// One degree of the backward transform with fixed-point swaps and beta
+// rotation; the alpha rotation and r-power scale stay in float-float.
+template <int G, int NA, int ACC>
+__device__ __forceinline__ void backward_degree_fixed(float2 *b, int n, int rowpad, const int *__restrict__ WRq,
+                                                      const ff *__restrict__ eout, ff f, int q,
+                                                      const Trig<arith<ff>, ACC> &tg, const FixTrig<ACC> &tq)
+{
+    using AR = arith<ff>;
+    const int d = n + 1;
+    float2 *bre = b + n * (n + 1);
+    float2 *bim = b + (n + 1) * (n + 1);
+    ff vr[NA], vi[NA];
+    float mx = 0.f;
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        const int m = q + G * a;
+        vr[a] = vi[a] = AR::zero();
+        if (m < d) {
+            vr[a] = AR::ld(bre + m);
+            vi[a] = AR::ld(bim + m);
+            mx = fmaxf(mx, fmaxf(fabsf(vr[a].hi), fabsf(vi[a].hi)));
+        }
+    }
+    int E = block_exponent(group_max<G>(mx));
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        const int m = q + G * a;
+        if (m < d) {
+            st_fixed(bre + m, ff_to_fixed(vr[a], E));
+            st_fixed(bim + m, ff_to_fixed(vi[a], E));
+        }
+    }
+    __syncwarp();
+    const int R = (d + rowpad - 1) & ~(rowpad - 1);
+    const int *WIq = WRq + ((d + 3) >> 1) * R;
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        long long ar[NA], ai[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) ar[a] = ai[a] = 0;
+        swap_both_fixed<G, NA>(WRq, WIq, R, bre, bim, d, n, q, ar, ai);
+        unsigned long long am = 0;
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            const unsigned long long ur = (unsigned long long)llabs(ar[a]), ui = (unsigned long long)llabs(ai[a]);
+            am = ur > am ? ur : am;
+            am = ui > am ? ui : am;
+        }
+        const int sh = renorm_shift(group_max<G>(am), kFixBits);
+        E += sh - 30;
+        __syncwarp();
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            const int ii = q + G * a;
+            if (ii < d) {
+                const int xr = round_shift(ar[a], sh), xi = round_shift(ai[a], sh);
+                if (pass == 0) {  // e^{-i m beta}
+                    st_fixed(bre + ii, rot_q30(tq.c[a], xr, -tq.s[a], xi));
+                    st_fixed(bim + ii, rot_q30(tq.c[a], xi, tq.s[a], xr));
+                } else {  // e^{-i m alpha}, back to the solid basis, r-power scale
+                    const ff ur = fixed_to_ff(xr, E), ui = fixed_to_ff(xi, E);
+                    const ff g = AR::mul(f, AR::ldt(eout + ii));
+                    const ff gc = AR::mul(g, tg.ca[a]), gs = AR::mul(g, tg.sa[a]);
+                    AR::st(bre + ii, AR::dot2(gc, ur, gs, ui));
+                    AR::st(bim + ii, AR::dot2(gc, ui, AR::neg(gs), ur));
+                }
             }
         }
         __syncwarp();
@@ -302,7 +459,97 @@ __device__ __forceinline__ void z_column(typename AR::Stor *b, const typename AR
     __syncwarp();
 }
 
-template <class A, int G, int ACC>
+// e^{i q gamma} by binary powers of e^{i gamma}, then steps of e^{i G gamma}:
+// the rotation factors of the elements m = q + G a a thread owns.
+template <int G, int ACC, class C, class Mul, class Out>
+__device__ __forceinline__ void rotation_powers(C ea, C eb, C one, int q, Mul cmul_, Out out)
+{
+    C pa = one, pb = one, ka = ea, kb = eb;
+#pragma unroll
+    for (int bit = 1; bit < G; bit <<= 1) {
+        if (q & bit) {
+            pa = cmul_(pa, ka);
+            pb = cmul_(pb, kb);
+        }
+        ka = cmul_(ka, ka);
+        kb = cmul_(kb, kb);
+    }
+#pragma unroll
+    for (int a = 0; a < ACC; ++a) {
+        out(a, pa, pb);
+        if (a + 1 < ACC) {
+            pa = cmul_(pa, ka);
+            pb = cmul_(pb, kb);
+        }
+    }
+}
+
+struct cff {
+    ff c, s;
+};
+
+// Per-thread geometry of one translation: |shift|, its inverse and the
+// rotation factors.  FP64 for the FP64 and FP32 kernels; float-float for the
+// split kernels, which then execute no FP64 instruction here (GB300's FP64
+// pipe runs at 1/64 of the FP32 rate).
+template <class AR, int G, int ACC, bool FIX>
+struct Geometry {
+    using T = typename AR::T;
+    T r, rinv;           // |shift| and 1/|shift| in the arithmetic
+    double rd, rinvd;    // the same in FP64 (FP64 and FP32 kernels)
+    Trig<AR, ACC> tg;
+    FixTrig<ACC> tq;
+
+    __device__ __forceinline__ Geometry(double x, double y, double z, int q)
+    {
+        if constexpr (AR::split) {
+            using A = arith<ff>;
+            const ff fx = ff_from_d_int(x), fy = ff_from_d_int(y), fz = ff_from_d_int(z);
+            const ff rxy2 = A::dot2(fx, fx, fy, fy);
+            const ff rxy = ff_sqrt(rxy2);
+            r = ff_sqrt(A::add(rxy2, A::mul(fz, fz)));
+            rinv = ff_rcp(r);
+            rd = rinvd = 0.0;
+            cff ea{ff{1.f, 0.f}, ff{0.f, 0.f}};
+            if (rxy.hi > 0.f) {
+                const ff rr = ff_rcp(rxy);
+                ea = cff{A::mul(fy, rr), A::mul(fx, rr)};
+            }
+            const cff eb{A::mul(fz, rinv), A::neg(A::mul(rxy, rinv))};
+            auto cm = [](cff a, cff b) {
+                return cff{A::dot2(a.c, b.c, A::neg(a.s), b.s), A::dot2(a.s, b.c, a.c, b.s)};
+            };
+            rotation_powers<G, ACC>(ea, eb, cff{ff{1.f, 0.f}, ff{0.f, 0.f}}, q, cm, [&](int a, cff pa, cff pb) {
+                tg.ca[a] = pa.c;
+                tg.sa[a] = pa.s;
+                tg.cb[a] = pb.c;
+                tg.sb[a] = pb.s;
+                if constexpr (FIX) {  // Q1.30
+                    tq.c[a] = __float2int_rn(pb.c.hi * 1073741824.f) + __float2int_rn(pb.c.lo * 1073741824.f);
+                    tq.s[a] = __float2int_rn(pb.s.hi * 1073741824.f) + __float2int_rn(pb.s.lo * 1073741824.f);
+                }
+            });
+        } else {
+            const double rxy = hypot(x, y);
+            rd = hypot(rxy, z);
+            rinvd = 1.0 / rd;
+            r = AR::from_d(rd);
+            rinv = AR::from_d(rinvd);
+            const cd ea = (rxy == 0) ? cd{1.0, 0.0} : cd{y / rxy, x / rxy};
+            const cd eb = cd{z * rinvd, -rxy * rinvd};
+            rotation_powers<G, ACC>(ea, eb, cd{1.0, 0.0}, q, [](cd a, cd b) { return cmul(a, b); },
+                                    [&](int a, cd pa, cd pb) {
+                                        tg.ca[a] = AR::from_d(pa.c);
+                                        tg.sa[a] = AR::from_d(pa.s);
+                                        tg.cb[a] = AR::from_d(pb.c);
+                                        tg.sb[a] = AR::from_d(pb.s);
+                                    });
+        }
+    }
+};
+
+// FIX selects block fixed-point swaps and beta rotations (float-float only).
+template <class A, int G, int ACC, bool FIX = false>
 __global__ void __launch_bounds__(256) k_translate(KParams p)
 {
     using AR = arith<A>;
@@ -311,6 +558,7 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
     using Src = typename src_of<A>::type;
     static_assert(sizeof(S) == sizeof(Src), "buffer slots hold one source value");
     static_assert(32 % G == 0, "a translation's threads must share a warp");
+    static_assert(!FIX || AR::split, "fixed-point swaps are a float-float variant");
 
     extern __shared__ __align__(16) unsigned char smem[];
     const int TS = p.TS;
@@ -393,13 +641,15 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         // 1. gather sources into the buffer (one warp per expansion, lanes over
         //    coefficients) in the arithmetic's storage format, zero past each
         //    source's order and in the padding (the swap loops read a few
-        //    slots past a row and multiply them by zero coefficients)
+        //    slots past a row and multiply them by zero coefficients).
+        //    Sources and targets stream through with evict-first hints so the
+        //    coefficient tables stay in the L1 left beside the buffers.
         for (int s = warp; s < TS; s += nwarps) {
             const int ps = (int)m_pin[s];
             const int cnt = ps * (ps + 1);
             const Src *sp = src + (long long)m_sidx[s] * p.sstride;
             S *bp = buf0 + (long long)s * p.spad;
-            for (int c = lane; c < p.spad; c += 32) AR::st(bp + c, c < cnt ? AR::from_d((double)sp[c]) : AR::zero());
+            for (int c = lane; c < p.spad; c += 32) AR::st(bp + c, c < cnt ? AR::from_src(__ldcs(sp + c)) : AR::zero());
         }
         __syncthreads();
 
@@ -407,36 +657,10 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         const int pin_w = __reduce_max_sync(FULL, pin);
         const int pout_w = __reduce_max_sync(FULL, pout);
 
-        // geometry in FP64 (euler, microkernel_generic.cpp:37-97)
-        const double rxy = hypot(x, y);
-        const double r = hypot(rxy, z);
-        const double rinv = 1.0 / r;
-        const cd ea = (rxy == 0) ? cd{1.0, 0.0} : cd{y / rxy, x / rxy};
-        const cd eb = cd{z * rinv, -rxy * rinv};
-        Trig<AR, ACC> tg;
-        {
-            // e^{i q gamma} by binary powers, then steps of e^{i G gamma}
-            cd pa{1.0, 0.0}, pb{1.0, 0.0}, ka = ea, kb = eb;
-            for (int bit = 1; bit < G; bit <<= 1) {
-                if (q & bit) {
-                    pa = cmul(pa, ka);
-                    pb = cmul(pb, kb);
-                }
-                ka = cmul(ka, ka);
-                kb = cmul(kb, kb);
-            }
-#pragma unroll
-            for (int a = 0; a < ACC; ++a) {
-                tg.ca[a] = AR::from_d(pa.c);
-                tg.sa[a] = AR::from_d(pa.s);
-                tg.cb[a] = AR::from_d(pb.c);
-                tg.sb[a] = AR::from_d(pb.s);
-                if (a + 1 < ACC) {
-                    pa = cmul(pa, ka);
-                    pb = cmul(pb, kb);
-                }
-            }
-        }
+        // geometry (euler, microkernel_generic.cpp:37-97)
+        Geometry<AR, G, ACC, FIX> geo(x, y, z, q);
+        const Trig<AR, ACC> &tg = geo.tg;
+        const FixTrig<ACC> &tq = geo.tq;
 
         // 2. forward transforms, degree by degree
         const bool Lin = (op == OP_L2L);
@@ -444,19 +668,26 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         // Float-float steps by repeated multiplication (FP32 pipe, error
         // ~n 2^-48); FP64 and FP32 take every power from the FP64 product.
         constexpr bool kFF = AR::split;
-        double rp = Lin ? 1.0 : rinv;
-        const double rpstep = Lin ? r : rinv;
-        T f = AR::from_d(rp);
-        const T rstep = AR::from_d(rpstep);
+        double rp = Lin ? 1.0 : geo.rinvd;
+        const double rpstep = Lin ? geo.rd : geo.rinvd;
+        T f = Lin ? AR::from_d(1.0) : geo.rinv;
+        const T rstep = Lin ? geo.r : geo.rinv;
         for (int n = 0; n < pin_w; ++n) {
             if (!kFF) f = AR::from_d(rp);
             const T *ein = EIN + n * (n + 1) / 2;
-            const T *WR = W + __ldg(p.woff + n);
-            dispatch<ACC>((n + G) / G, [&](auto na) {
-                forward_degree<AR, G, decltype(na)::value, ACC>(b, n, p.rowpad, WR, ein, f, q, tg);
-            });
+            if constexpr (FIX) {
+                const int *WRq = p.Wq + __ldg(p.woff + n);
+                dispatch<ACC>((n + G) / G, [&](auto na) {
+                    forward_degree_fixed<G, decltype(na)::value, ACC>(b, n, p.rowpad, WRq, ein, f, q, tg, tq);
+                });
+            } else {
+                const T *WR = W + __ldg(p.woff + n);
+                dispatch<ACC>((n + G) / G, [&](auto na) {
+                    forward_degree<AR, G, decltype(na)::value, ACC>(b, n, p.rowpad, WR, ein, f, q, tg);
+                });
+            }
             if (kFF) f = AR::mul(f, rstep);
-            rp *= rpstep;
+            if (!kFF) rp *= rpstep;
         }
 
         // 3. z-translation, column by column.  Columns m >= min(P_in, P_out)
@@ -477,20 +708,27 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
 
         // 4. backward transforms
         const bool Mout = (op == OP_M2M);
-        double rq = Mout ? r : 1.0;  // r^(n+1) (M output) or r^-n (L output)
-        const double rqstep = Mout ? r : rinv;
-        T fo = AR::from_d(rq);
-        const T qstep = AR::from_d(rqstep);
+        double rq = Mout ? geo.rd : 1.0;  // r^(n+1) (M output) or r^-n (L output)
+        const double rqstep = Mout ? geo.rd : geo.rinvd;
+        T fo = Mout ? geo.r : AR::from_d(1.0);
+        const T qstep = Mout ? geo.r : geo.rinv;
         for (int n = 0; n < nout_w; ++n) {
             if (!kFF) fo = AR::from_d(rq);
             const T f = fo;
             const T *eo = EOUT + n * (n + 1) / 2;
-            const T *WR = W + __ldg(p.woff + n);
-            dispatch<ACC>((n + G) / G, [&](auto na) {
-                backward_degree<AR, G, decltype(na)::value, ACC>(b, n, p.rowpad, WR, eo, f, q, tg);
-            });
+            if constexpr (FIX) {
+                const int *WRq = p.Wq + __ldg(p.woff + n);
+                dispatch<ACC>((n + G) / G, [&](auto na) {
+                    backward_degree_fixed<G, decltype(na)::value, ACC>(b, n, p.rowpad, WRq, eo, f, q, tg, tq);
+                });
+            } else {
+                const T *WR = W + __ldg(p.woff + n);
+                dispatch<ACC>((n + G) / G, [&](auto na) {
+                    backward_degree<AR, G, decltype(na)::value, ACC>(b, n, p.rowpad, WR, eo, f, q, tg);
+                });
+            }
             if (kFF) fo = AR::mul(fo, qstep);
-            rq *= rqstep;
+            if (!kFF) rq *= rqstep;
         }
         __syncthreads();
 
@@ -504,11 +742,24 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             const Src *sp = src + (long long)m_sidx[s] * p.sstride;
             Src *dp = dst + (long long)m_tidx[s] * p.dstride;
             for (int c = lane; c < cnt; c += 32) {
-                double v = 0;
-                if (c < po * (po + 1)) v = AR::to_d(AR::ld(bp + c));
-                if (c < pid * (pid + 1)) v += (double)sp[c];
-                if (p.atomic) atomicAdd(dp + c, (Src)v);
-                else dp[c] = (Src)((double)dp[c] + v);
+                if constexpr (AR::split) {
+                    // hi and lo widen by exponent re-biasing; two FP64 additions
+                    double v = p.atomic ? 0.0 : (double)__ldcs(dp + c);
+                    if (c < po * (po + 1)) {
+                        const T t = AR::ld(bp + c);
+                        const double hd = d_from_f_int(t.hi), lo = d_from_f_int(t.lo);
+                        v = p.atomic ? hd + lo : (v + hd) + lo;
+                    }
+                    if (c < pid * (pid + 1)) v += (double)__ldcs(sp + c);
+                    if (p.atomic) atomicAdd(dp + c, (Src)v);
+                    else __stcs(dp + c, (Src)v);
+                } else {
+                    double v = 0;
+                    if (c < po * (po + 1)) v = AR::to_d(AR::ld(bp + c));
+                    if (c < pid * (pid + 1)) v += (double)__ldcs(sp + c);
+                    if (p.atomic) atomicAdd(dp + c, (Src)v);
+                    else __stcs(dp + c, (Src)((double)__ldcs(dp + c) + v));
+                }
             }
         }
         __syncthreads();

@@ -7,7 +7,11 @@ Tolerances (relative L2 per target expansion, max over the batch):
     the reference itself sits ~1e-13..1e-11 from the exact formula at these
     orders, and our orthogonal-basis arithmetic differs from its packed
     checkerboard arithmetic only by rounding.
-  * split (float-float) vs the reference's double outputs: 1e-10 raw.
+  * split (block fixed-point rotations, float-float z-translation) vs the
+    reference's double outputs: 1e-7 in the orthonormal basis, the split
+    mode's accuracy contract.
+  * split_ff (float-float throughout) vs the reference's double outputs:
+    1e-10 raw.
   * plain FP32 vs the FP64 oracle: no worse than 4x the reference's own
     float error on the same inputs, plus 1e-6 in the orthonormal basis.
 """
@@ -35,7 +39,7 @@ def _names(tag):
 
 
 @pytest.mark.parametrize("name", _names("f64"))
-@pytest.mark.parametrize("precision", [0, 1], ids=["plain", "split"])
+@pytest.mark.parametrize("precision", [0, 1, 2], ids=["plain", "split", "split_ff"])
 def test_golden_f64(ctxs, name, precision):
     c = CASES[name]
     op = str(c["op"])
@@ -43,8 +47,12 @@ def test_golden_f64(ctxs, name, precision):
     got = run_device(ctxs[("f64", 16)], op, precision, c["src"], c["dst0"], c["Pin"], c["Pout"], c["xyz"],
                      c["sidx"], c["tidx"], repeat=repeat, order_bound=int(c["Pop"]))
     g, r = _contrib(c, got)
-    tol = 1e-11 if precision == 0 else 1e-10
-    err = rel_err(g, r)
+    if precision == 1:
+        err = rel_err(g, r, norm_weights(int(c["Pop"]), "M" if op == "m2m" else "L"))
+        tol = 1e-7
+    else:
+        err = rel_err(g, r)
+        tol = 1e-11 if precision == 0 else 1e-10
     assert err < tol, f"{name}: rel err {err:.3e}"
 
 
