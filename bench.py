@@ -46,6 +46,11 @@ WORKLOADS = {
 
 METRIC = "M2L translations/s at P=16, chosen vs plain FP64 GPU at equal rel. error; %roofline"
 
+# HBM traffic per translation of the split kernel from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum over the launch / 65 536
+# translations, workload m2l16_small); see profiles/
+TRAFFIC = {("m2l", 16): 5716.0}
+
 
 def useful_flops(op, P):
     """Algorithmic flops of one translation (rotations + z-translation), equal orders."""
@@ -194,7 +199,7 @@ def accuracy(ctx, op, P, src, shift, pin, nsub, dev):
                    sh.cpu().numpy())
     w = norm_weights(P, "M" if op == "m2m" else "L")
     out = {}
-    for name, prec in (("plain_fp64", 0), ("split", 1)):
+    for name, prec in (("plain_fp64", 0), ("split", 1), ("split_ff", 2)):
         d = torch.zeros(nsub, S, dtype=torch.float64, device=dev)
         ctx.translate_device(op, prec, nsub, s, S, nsub, d, S, nsub, pi, pi, sh)
         torch.cuda.synchronize()
@@ -325,8 +330,10 @@ def main():
     clocks = Clocks(local)
     ms_split, launches, clk = timed(1, args.steps, args.warmup, clocks)
     ms_plain, _, _ = timed(0, max(2, args.steps // 2), 1)
+    ms_ff, _, _ = timed(2, max(2, args.steps // 2), 1)
     value = world * N / (ms_split * 1e-3)
     plain_value = world * N / (ms_plain * 1e-3)
+    ff_value = world * N / (ms_ff * 1e-3)
 
     # end to end through the C ABI with pinned host buffers
     h_src = torch.empty(N, S, dtype=torch.float64, pin_memory=True)
@@ -360,17 +367,22 @@ def main():
         with open(mp) as f:
             hbm_peak = json.load(f).get("hbm_gbs", hbm_peak)
         peak_src = "measured"
+    tb = TRAFFIC.get((op, P))
     roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_source": peak_src,
-            "kernel": "k_translate<ff,4> (split)", "bytes_per_translation": B}
-    ff_ops_per_flop = 5.5  # float-float multiply-add: 11 FP32 operations for 2 flops
+            "frac": achieved_gbs / hbm_peak, "traffic": tb * N if tb else None,
+            "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the split kernel, "
+                               f"{tb:.0f} B per translation on 65 536 translations, scaled to {N}") if tb else None,
+            "peak_source": peak_src, "kernel": "k_translate<ff, G, ACC, fixed> (split)",
+            "bytes_per_translation": B}
+    # the split path does FP64-class work on the FP32 and integer pipes: its
+    # useful flop rate set against the FP64 pipe's measured peak (a ratio
+    # above 1 is beyond any FP64 kernel's reach)
     roof_compute = {
-        "pipe": "fp32 (float-float arithmetic)",
+        "basis": "useful flops of the rotation method per translation (2 per multiply-add)",
         "useful_flops_per_translation": F,
-        "fp32_ops_per_translation": F * ff_ops_per_flop,
-        "achieved_tflops": F * ff_ops_per_flop / t_kernel / 1e12,
-        "peak_tflops": peaks["fp32"] / 1e12, "peak_source": "measured FFMA loop in this run",
-        "frac": F * ff_ops_per_flop / t_kernel / peaks["fp32"]}
+        "achieved_tflops": F / t_kernel / 1e12,
+        "fp64_peak_tflops": peaks["fp64"] / 1e12, "frac_of_fp64_peak": F / t_kernel / peaks["fp64"],
+        "fp32_peak_tflops": peaks["fp32"] / 1e12, "peak_source": "measured DFMA / FFMA loops in this run"}
     roof_fp64 = {"kernel": "k_translate<double,4> (plain FP64)", "pipe": "fp64",
                  "achieved_tflops": F * plain_value / world / 1e12, "peak_tflops": peaks["fp64"] / 1e12,
                  "frac": F * plain_value / world / peaks["fp64"], "peak_source": "measured DFMA loop in this run"}
@@ -386,11 +398,15 @@ def main():
                          f"{'reference multithreaded_translator' if use_ref else 'oracle port, one pthread per core'}"}
     line = {"metric": METRIC, "value": value, "unit": "translations/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_split, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32x2 (float-float) swaps/rotations/z-translation, f64 geometry and "
-                                          "accumulation", "data": "synthetic (seeded P2M of random charges)",
+            "vs_baseline": None,
+            "dtype": "split: int32 block fixed point (swaps, polar rotations), f32x2 float-float (z-translation, "
+                     "azimuthal rotations, scaling, geometry), f64 accumulation",
+            "data": "synthetic (seeded P2M of random charges)",
             "config": config,
             "plain_fp64": {"value": plain_value, "ms_per_step": ms_plain},
             "split_over_plain_fp64": value / plain_value,
+            "split_ff": {"value": ff_value, "ms_per_step": ms_ff,
+                         "note": "float-float throughout (relative error ~1e-13)"},
             "accuracy_vs_fp64_oracle_1000": acc,
             "e2e": {"value": world * N / e2e_s, "unit": "translations/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "sfmm_translate_host_packed (pinned host buffers)"},

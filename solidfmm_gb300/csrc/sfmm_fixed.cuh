@@ -33,17 +33,6 @@ __device__ __forceinline__ float group_max(float v)
     return v;
 }
 
-template <int G>
-__device__ __forceinline__ unsigned long long group_max(unsigned long long v)
-{
-#pragma unroll
-    for (int o = 1; o < G; o <<= 1) {
-        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w > v ? w : v;
-    }
-    return v;
-}
-
 // Mantissa width after every renormalisation: |m| <= 2^kFixBits (the
 // overflow bound above holds for kFixBits <= 30 and degrees below 28).
 constexpr int kFixBits = 30;
@@ -71,12 +60,23 @@ __device__ __forceinline__ ff fixed_to_ff(int m, int E)
     return ff{ldexp2(hi, E), ldexp2(lo, E)};
 }
 
-// Shift that brings int64 accumulators whose largest magnitude is mx to
-// at most `bits` bits (the block exponent grows by the shift).
-__device__ __forceinline__ int renorm_shift(unsigned long long mx, int bits)
+// Shift that brings the int64 accumulators of one degree row (all G threads
+// of the translation) to at most kFixBits bits; the block exponent grows by
+// the shift.  The bit length comes from the OR of one's-complement
+// magnitudes: v ^ (v >> 63) is |v| or |v| - 1, whose bit length can only
+// undercount for v = -2^k, which then narrows to exactly -2^kFixBits.  The
+// group maximum runs on the 32-bit bit lengths.
+template <int G, int NA>
+__device__ __forceinline__ int group_renorm_shift(const long long (&ar)[NA], const long long (&ai)[NA])
 {
-    const int used = 64 - __clzll((long long)mx);
-    return used > bits ? used - bits : 0;
+    unsigned long long o = 0;
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+        o |= (unsigned long long)(ar[a] ^ (ar[a] >> 63)) | (unsigned long long)(ai[a] ^ (ai[a] >> 63));
+    int used = 64 - __clzll((long long)o);
+#pragma unroll
+    for (int k = 1; k < G; k <<= 1) used = max(used, __shfl_xor_sync(0xffffffffu, used, k));
+    return used > kFixBits ? used - kFixBits : 0;
 }
 
 __device__ __forceinline__ int round_shift(long long a, int s)
@@ -93,25 +93,24 @@ __device__ __forceinline__ int rot_q30(int c, int x, int s, int y)
 
 // Integer swap of one degree, both parts: rows i = q + G a (a < NA) of the
 // Q1.30 matrices applied to the int32 mantissas stored in the buffer slots
-// (low word of each 8-byte slot).  Same column pattern, padding and
-// software pipelining as the floating-point swap.
-template <int G, int NA>
-__device__ __forceinline__ void swap_both_fixed(const int *__restrict__ WR, const int *__restrict__ WI, int R,
-                                                const float2 *xre, const float2 *xim, int d, int n, int q,
-                                                long long (&ar)[NA], long long (&ai)[NA])
+// (low word of each 8-byte slot).  Same coefficient layout (slot t: R rows of
+// W_R, then R rows of W_I), padding and software pipelining as the
+// floating-point swap.
+template <int G, int NA, int R>
+__device__ __forceinline__ void swap_both_fixed(const int *__restrict__ W, const float2 *xre, const float2 *xim,
+                                                int d, int n, int q, long long (&ar)[NA], long long (&ai)[NA])
 {
     const int jr0 = (q + n) & 1, ji0 = jr0 ^ 1;
     const int cnt = (d + 1) >> 1;
-    const int *wr_p = WR + q;
-    const int *wi_p = WI + q;
+    const int *w = W + q;
     const int *xr_p = reinterpret_cast<const int *>(xre + jr0);
     const int *xi_p = reinterpret_cast<const int *>(xim + ji0);
     int xrn = *xr_p, xin = *xi_p;
     int wrn[NA], win[NA];
 #pragma unroll
     for (int a = 0; a < NA; ++a) {
-        wrn[a] = __ldg(wr_p + G * a);
-        win[a] = __ldg(wi_p + G * a);
+        wrn[a] = __ldg(w + G * a);
+        win[a] = __ldg(w + R + G * a);
     }
 #pragma unroll 2
     for (int t = 0; t < cnt; ++t) {
@@ -124,14 +123,13 @@ __device__ __forceinline__ void swap_both_fixed(const int *__restrict__ WR, cons
         }
         xr_p += 4;  // two 8-byte slots
         xi_p += 4;
-        wr_p += R;
-        wi_p += R;
+        w += 2 * R;
         xrn = *xr_p;
         xin = *xi_p;
 #pragma unroll
         for (int a = 0; a < NA; ++a) {
-            wrn[a] = __ldg(wr_p + G * a);
-            win[a] = __ldg(wi_p + G * a);
+            wrn[a] = __ldg(w + G * a);
+            win[a] = __ldg(w + R + G * a);
         }
 #pragma unroll
         for (int a = 0; a < NA; ++a) {

@@ -56,7 +56,7 @@ double w_entry(const HostTables &t, int n, int part, int i, int j)
     if (i < 0 || j < 0 || i >= d || j >= d) return 0.0;
     const bool rnz = ((i + j + n) & 1) == 0;
     if (rnz != (part == 0)) return 0.0;
-    return t.W[t.woff[n] + (part ? size_t(wcols(d)) * R : 0) + size_t(j >> 1) * R + i];
+    return t.W[t.woff[n] + size_t(j >> 1) * 2 * R + (part ? R : 0) + i];
 }
 
 HostTables build_tables(int P)
@@ -85,8 +85,8 @@ HostTables build_tables(int P)
         auto D = [&](int m) { return sf(n - m) * sf(n + m); };
         auto E = [&](int m) { return m == 0 ? D(0) / s2 : D(m); };
         const int R = wrows(d, pad);
-        double *WR = &t.W[t.woff[n]];
-        double *WI = WR + size_t(wcols(d)) * R;
+        double *WR = &t.W[t.woff[n]];  // slot t: W_R rows at 2tR, W_I rows at 2tR + R
+        double *WI = WR + R;
         for (int i = 0; i < d; ++i)       // output row (coefficient m = i)
             for (int j = 0; j < d; ++j) { // input column (coefficient l = j)
                 // the reference's real/imag combinations (operator_data.cpp:99-147)
@@ -98,7 +98,7 @@ HostTables build_tables(int P)
                 else imf = Bv(j, i) - Bv(-j, i);
                 // keep only the checkerboard the reference stores
                 const bool rnz = ((i + j + n) & 1) == 0;
-                const size_t slot = size_t(j >> 1) * R + i;  // j = jr(i) + 2t or ji(i) + 2t
+                const size_t slot = size_t(j >> 1) * 2 * R + i;  // j = jr(i) + 2t or ji(i) + 2t
                 if (rnz) WR[slot] = rf * (E(i) / E(j));
                 else if (i > 0 && j > 0) WI[slot] = imf * (D(i) / D(j));
             }

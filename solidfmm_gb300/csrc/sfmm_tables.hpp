@@ -24,14 +24,14 @@ namespace sfmm {
 
 struct HostTables {
     int P = 0;
-    // W for degree n (d = n+1): R block at woff[n], I block at woff[n] +
-    // wcols(d)*wrows(d,pad).  Only the checkerboard a swap uses is stored:
-    // W_R(i, j) is nonzero only for j = jr(i) + 2t with jr(i) = (i+n) & 1,
-    // W_I(i, j) only for j = ji(i) + 2t with ji(i) = jr(i) ^ 1; slot t of row
-    // i sits at t*wrows(d,pad) + i.  Rows are padded to a multiple of
-    // row_pad(P) and slots to wcols(d) = (d+3)/2 with zeros (the swap loops
-    // prefetch one slot past the last column), so the kernels load
-    // coefficients without bounds checks.
+    // W for degree n (d = n+1) at woff[n].  Only the checkerboard a swap
+    // uses is stored: W_R(i, j) is nonzero only for j = jr(i) + 2t with
+    // jr(i) = (i+n) & 1, W_I(i, j) only for j = ji(i) + 2t with
+    // ji(i) = jr(i) ^ 1.  Slot t holds R = wrows(d,pad) rows of W_R (row i at
+    // 2tR + i) followed by R rows of W_I (at 2tR + R + i).  Rows are padded
+    // to a multiple of row_pad(P) and slots to wcols(d) = (d+3)/2 with zeros
+    // (the swap loops prefetch one slot past the last column), so the
+    // kernels load coefficients without bounds checks.
     int pad = 8;
     std::vector<double> W;
     std::vector<int> woff;

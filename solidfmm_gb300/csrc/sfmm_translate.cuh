@@ -76,33 +76,46 @@ __device__ __forceinline__ void dispatch(int na, F &&f)
     }
 }
 
+// Rows of a degree's swap-coefficient block in the instance that runs NA
+// accumulator blocks of G threads: the tables pad rows to a multiple of 8
+// for orders up to 32 (G = 4 or 8) and of 32 above (G = 32), so the row
+// count of every degree served by one (G, NA) instance is the same
+// compile-time constant.
+template <int G, int NA>
+__host__ __device__ constexpr int swap_rows()
+{
+    return G == 32 ? 32 * NA : ((G * NA + 7) & ~7);
+}
+
 // Both swap parts of one degree: rows i = q + G a (a < NA) of W_R applied to
 // the real parts (columns j = jr, jr+2, ...) and of W_I to the imaginary
 // parts (the complementary checkerboard, columns ji = jr^1, ji+2, ...).
-// The coefficient blocks hold only that checkerboard (slot t of row i is
-// column jr(i) + 2t), zero-padded (rows to a multiple of 8, slots to
-// (d+3)/2), and the buffer slots past each expansion are zero, so every load
-// is unconditional; operands of the next column pair are fetched before the
+// The coefficient block holds only that checkerboard: slot t of row i is
+// column jr(i) + 2t (W_R) or ji(i) + 2t (W_I), and each slot stores the R
+// rows of W_R followed by the R rows of W_I, so one pointer walks both with
+// compile-time offsets.  Rows are zero-padded to R and slots to (d+3)/2, and
+// the buffer slots past each expansion are zero, so every load is
+// unconditional; operands of the next column pair are fetched before the
 // current pair's multiply-adds (software pipelining), and the real and
 // imaginary chains are independent (2*NA accumulations per iteration).
 template <class AR, int G, int NA>
-__device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ WR, const typename AR::T *__restrict__ WI,
-                                          int R, const typename AR::Stor *xre, const typename AR::Stor *xim, int d,
-                                          int n, int q, typename AR::Acc (&ar)[NA], typename AR::Acc (&ai)[NA])
+__device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ W, const typename AR::Stor *xre,
+                                          const typename AR::Stor *xim, int d, int n, int q,
+                                          typename AR::Acc (&ar)[NA], typename AR::Acc (&ai)[NA])
 {
     using T = typename AR::T;
+    constexpr int R = swap_rows<G, NA>();
     const int jr0 = (q + n) & 1, ji0 = jr0 ^ 1;
     const int cnt = (d + 1) >> 1;  // iterations of the longer part
-    const T *wr_p = WR + q;
-    const T *wi_p = WI + q;
+    const T *w = W + q;
     const typename AR::Stor *xr_p = xre + jr0;
     const typename AR::Stor *xi_p = xim + ji0;
     T xrn = AR::ld(xr_p), xin = AR::ld(xi_p);
     T wrn[NA], win[NA];
 #pragma unroll
     for (int a = 0; a < NA; ++a) {
-        wrn[a] = AR::ldt(wr_p + G * a);
-        win[a] = AR::ldt(wi_p + G * a);
+        wrn[a] = AR::ldt(w + G * a);
+        win[a] = AR::ldt(w + R + G * a);
     }
 #pragma unroll 2
     for (int t = 0; t < cnt; ++t) {
@@ -115,14 +128,13 @@ __device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ WR,
         }
         xr_p += 2;
         xi_p += 2;
-        wr_p += R;
-        wi_p += R;
+        w += 2 * R;
         xrn = AR::ld(xr_p);
         xin = AR::ld(xi_p);
 #pragma unroll
         for (int a = 0; a < NA; ++a) {
-            wrn[a] = AR::ldt(wr_p + G * a);
-            win[a] = AR::ldt(wi_p + G * a);
+            wrn[a] = AR::ldt(w + G * a);
+            win[a] = AR::ldt(w + R + G * a);
         }
 #pragma unroll
         for (int a = 0; a < NA; ++a) {
@@ -165,8 +177,6 @@ __device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, int 
         }
     }
     __syncwarp();
-    const int R = (d + rowpad - 1) & ~(rowpad - 1);
-    const T *WI = WR + ((d + 3) >> 1) * R;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         Acc ar[NA], ai[NA];
@@ -175,7 +185,7 @@ __device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, int 
             ar[a] = AR::acc0();
             ai[a] = AR::acc0();
         }
-        swap_both<AR, G, NA>(WR, WI, R, bre, bim, d, n, q, ar, ai);
+        swap_both<AR, G, NA>(WR, bre, bim, d, n, q, ar, ai);
         __syncwarp();
 #pragma unroll
         for (int a = 0; a < NA; ++a) {
@@ -210,8 +220,6 @@ __device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, int
     const int d = n + 1;
     S *bre = b + n * (n + 1);
     S *bim = b + (n + 1) * (n + 1);
-    const int R = (d + rowpad - 1) & ~(rowpad - 1);
-    const T *WI = WR + ((d + 3) >> 1) * R;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         Acc ar[NA], ai[NA];
@@ -220,7 +228,7 @@ __device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, int
             ar[a] = AR::acc0();
             ai[a] = AR::acc0();
         }
-        swap_both<AR, G, NA>(WR, WI, R, bre, bim, d, n, q, ar, ai);
+        swap_both<AR, G, NA>(WR, bre, bim, d, n, q, ar, ai);
         __syncwarp();
 #pragma unroll
         for (int a = 0; a < NA; ++a) {
@@ -296,22 +304,13 @@ __device__ __forceinline__ void forward_degree_fixed(float2 *b, int n, int rowpa
         }
     }
     __syncwarp();
-    const int R = (d + rowpad - 1) & ~(rowpad - 1);
-    const int *WIq = WRq + ((d + 3) >> 1) * R;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         long long ar[NA], ai[NA];
 #pragma unroll
         for (int a = 0; a < NA; ++a) ar[a] = ai[a] = 0;
-        swap_both_fixed<G, NA>(WRq, WIq, R, bre, bim, d, n, q, ar, ai);
-        unsigned long long am = 0;
-#pragma unroll
-        for (int a = 0; a < NA; ++a) {
-            const unsigned long long ur = (unsigned long long)llabs(ar[a]), ui = (unsigned long long)llabs(ai[a]);
-            am = ur > am ? ur : am;
-            am = ui > am ? ui : am;
-        }
-        const int sh = renorm_shift(group_max<G>(am), kFixBits);
+        swap_both_fixed<G, NA, swap_rows<G, NA>()>(WRq, bre, bim, d, n, q, ar, ai);
+        const int sh = group_renorm_shift<G, NA>(ar, ai);
         E += sh - 30;
         __syncwarp();
 #pragma unroll
@@ -365,22 +364,13 @@ __device__ __forceinline__ void backward_degree_fixed(float2 *b, int n, int rowp
         }
     }
     __syncwarp();
-    const int R = (d + rowpad - 1) & ~(rowpad - 1);
-    const int *WIq = WRq + ((d + 3) >> 1) * R;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
         long long ar[NA], ai[NA];
 #pragma unroll
         for (int a = 0; a < NA; ++a) ar[a] = ai[a] = 0;
-        swap_both_fixed<G, NA>(WRq, WIq, R, bre, bim, d, n, q, ar, ai);
-        unsigned long long am = 0;
-#pragma unroll
-        for (int a = 0; a < NA; ++a) {
-            const unsigned long long ur = (unsigned long long)llabs(ar[a]), ui = (unsigned long long)llabs(ai[a]);
-            am = ur > am ? ur : am;
-            am = ui > am ? ui : am;
-        }
-        const int sh = renorm_shift(group_max<G>(am), kFixBits);
+        swap_both_fixed<G, NA, swap_rows<G, NA>()>(WRq, bre, bim, d, n, q, ar, ai);
+        const int sh = group_renorm_shift<G, NA>(ar, ai);
         E += sh - 30;
         __syncwarp();
 #pragma unroll
@@ -421,23 +411,21 @@ __device__ __forceinline__ void z_column(typename AR::Stor *b, const typename AR
         ai[a] = AR::acc0();
     }
     if (kbeg < kend) {
-        int k = kbeg;
-        const T *h_p = Hm + (long long)(k - m) * HR + q;
-        T xrn = AR::ld(b + k * (k + 1) + m);
-        T xin = AR::ld(b + (k + 1) * (k + 1) + m);
-        T hn[NA];
+        // row k of column m: real part at ro = k(k+1) + m, imaginary part at
+        // ro + k + 1; both advance by 2(k+1) per row
+        const T *h_p = Hm + (long long)(kbeg - m) * HR + q;
+        int ro = kbeg * (kbeg + 1) + m, step = 2 * (kbeg + 1);
+        T xr = AR::ld(b + ro), xi = AR::ld(b + ro + kbeg + 1);
+        T hc[NA];
 #pragma unroll
-        for (int a = 0; a < NA; ++a) hn[a] = AR::ldt(h_p + G * a);
+        for (int a = 0; a < NA; ++a) hc[a] = AR::ldt(h_p + G * a);
 #pragma unroll 2
-        for (; k < kend; ++k) {
-            const T xr = xrn, xi = xin;
-            T hc[NA];
-#pragma unroll
-            for (int a = 0; a < NA; ++a) hc[a] = hn[a];
-            const int kn = min(k + 1, kend - 1);  // the last prefetch reloads column kend-1
-            h_p = Hm + (long long)(kn - m) * HR + q;
-            xrn = AR::ld(b + kn * (kn + 1) + m);
-            xin = AR::ld(b + (kn + 1) * (kn + 1) + m);
+        for (int k = kbeg; k < kend - 1; ++k) {  // the operands of row k+1 load before row k's multiply-adds
+            ro += step;
+            step += 2;
+            h_p += HR;
+            const T xrn = AR::ld(b + ro), xin = AR::ld(b + ro + k + 2);
+            T hn[NA];
 #pragma unroll
             for (int a = 0; a < NA; ++a) hn[a] = AR::ldt(h_p + G * a);
 #pragma unroll
@@ -445,6 +433,15 @@ __device__ __forceinline__ void z_column(typename AR::Stor *b, const typename AR
                 AR::mac(ar[a], hc[a], xr);
                 AR::mac(ai[a], hc[a], xi);
             }
+            xr = xrn;
+            xi = xin;
+#pragma unroll
+            for (int a = 0; a < NA; ++a) hc[a] = hn[a];
+        }
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            AR::mac(ar[a], hc[a], xr);
+            AR::mac(ai[a], hc[a], xi);
         }
     }
     __syncwarp();
