@@ -42,6 +42,8 @@ WORKLOADS = {
     "m2l20": ("m2l", 20, 1_000_000, 128),
     "m2m20": ("m2m", 20, 1_000_000, 128),
     "l2l20": ("l2l", 20, 1_000_000, 128),
+    # 1.5e6 translations, 40% M2L / 30% M2M / 30% L2L, orders U{4..24}
+    "mixed": ("mixed", 24, 1_500_000, 64),
 }
 
 METRIC = "M2L translations/s at P=16, chosen vs plain FP64 GPU at equal rel. error; %roofline"
@@ -238,6 +240,142 @@ def cpu_leg(op, P, nq, seconds_target, seed, use_ref):
     return done / total, threads, ns, done
 
 
+MIXED_METRIC = "mixed M2L/M2M/L2L translations/s, orders U{4..24}, 1.5e6 per GPU"
+
+
+def run_mixed(args):
+    """Mixed-order batch: 40% M2L, 30% M2M, 30% L2L with P_in, P_out iid
+    U{4..24}, sources gathered from 65 536 P2M/P2L expansions per kind,
+    distinct targets.  One execution plan (three stages, order-sorted
+    segments, CUDA graph) against one unsorted launch per operator at order
+    bound 24 and against one launch per (operator, P_in, P_out) group."""
+    import torch
+    import solidfmm_gb300 as sf
+    from solidfmm_gb300 import build as _b
+
+    world, rank, local = dist_init(args)
+    _b.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    P, N = 24, WORKLOADS["mixed"][2]
+    S = P * (P + 1)
+    NS = 65536
+    ctx = sf.Context(P, "f64", device=local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    srcM, _, _ = make_inputs(ctx, "m2m", P, NS, 64, 500 + rank, dev)
+    srcL, _, _ = make_inputs(ctx, "l2l", P, NS, 64, 600 + rank, dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(700 + rank)
+    counts = {"m2l": int(0.4 * N), "m2m": int(0.3 * N)}
+    counts["l2l"] = N - counts["m2l"] - counts["m2m"]
+    dst = torch.zeros(N, S, dtype=torch.float64, device=dev)
+    batches = {}
+    off = 0
+    for op in ("m2l", "m2m", "l2l"):
+        n = counts[op]
+        pin = torch.randint(4, 25, (n,), device=dev, generator=g, dtype=torch.int32)
+        pout = torch.randint(4, 25, (n,), device=dev, generator=g, dtype=torch.int32)
+        sidx = torch.randint(0, NS, (n,), device=dev, generator=g, dtype=torch.int32)
+        if op == "m2l":
+            u = torch.randn(n, 3, dtype=torch.float64, device=dev, generator=g)
+            sh = u / u.norm(dim=1, keepdim=True) * (2 + 2 * torch.rand(n, 1, dtype=torch.float64, device=dev,
+                                                                          generator=g))
+        else:
+            sh = 0.5 * (torch.randint(0, 2, (n, 3), device=dev, generator=g).to(torch.float64) * 2 - 1)
+        batches[op] = dict(n=n, pin=pin, pout=pout, sidx=sidx, shift=sh.contiguous(), dst=dst[off:off + n],
+                           src=srcL if op == "l2l" else srcM)
+        off += n
+
+    def plan_for(prec):
+        pl = sf.Plan(ctx)
+        for op, b in batches.items():
+            pl.add(op, prec, b["n"], b["src"], S, NS, b["dst"], S, b["n"], b["pin"], b["pout"], b["shift"],
+                   src_index=b["sidx"])
+        return pl.finalize()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier(world)
+        l0 = ctx.launches
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        return allmax(world, e0.elapsed_time(e1) / steps, dev), (ctx.launches - l0) // max(steps, 1)
+
+    clocks = Clocks(local)
+    plan_split = plan_for(1)
+    clocks.start()
+    ms_plan, launches = timed(plan_split.run, args.steps, args.warmup)
+    clk = clocks.stop()
+    plan_plain = plan_for(0)
+    ms_plan_plain, _ = timed(plan_plain.run, max(2, args.steps // 2), 1)
+
+    def unsorted(prec):
+        def f():
+            for op, b in batches.items():
+                ctx.translate_device(op, prec, b["n"], b["src"], S, NS, b["dst"], S, b["n"], b["pin"], b["pout"],
+                                     b["shift"], src_index=b["sidx"], order_bound=P)
+        return f
+
+    ms_unsorted, _ = timed(unsorted(1), max(2, args.steps // 2), 1)
+    ms_unsorted_plain, _ = timed(unsorted(0), max(2, args.steps // 2), 1)
+
+    # one launch per (operator, P_in, P_out) group
+    groups = []
+    for op, b in batches.items():
+        key = (b["pin"].long() * 32 + b["pout"].long())
+        order = torch.argsort(key)
+        ks = key[order]
+        bounds = torch.nonzero(ks[1:] != ks[:-1]).flatten().cpu().tolist()
+        starts = [0] + [x + 1 for x in bounds]
+        ends = starts[1:] + [b["n"]]
+        kl = ks.cpu().tolist()
+        for s0, s1 in zip(starts, ends):
+            pi, po = divmod(kl[s0], 32)
+            idx = order[s0:s1]
+            groups.append((op, s1 - s0, max(pi, po), b["src"], b["sidx"][idx].contiguous(), b["dst"],
+                           idx.to(torch.int32).contiguous(), b["pin"][idx].contiguous(), b["pout"][idx].contiguous(),
+                           b["shift"][idx].contiguous(), b["n"]))
+
+    def per_pair(prec):
+        def f():
+            for op, n, bnd, src, si, d, ti, pi, po, sh, nd in groups:
+                ctx.translate_device(op, prec, n, src, S, NS, d, S, nd, pi, po, sh, src_index=si, dst_index=ti,
+                                     order_bound=bnd)
+        return f
+
+    ms_pairs, _ = timed(per_pair(1), 2, 1)
+    ms_pairs_plain, _ = timed(per_pair(0), 2, 1)
+    if rank != 0:
+        return
+    segs = plan_split.segments()
+    rate = lambda ms: world * N / (ms * 1e-3)  # noqa: E731
+    line = {"metric": MIXED_METRIC, "value": rate(ms_plan), "unit": "translations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_plan, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "split (int32 block fixed point rotations, float-float z-translation, f64 accumulation)",
+            "data": "synthetic (seeded P2M/P2L sources, random orders and shifts)",
+            "config": {"workload": "mixed: 600k M2L + 450k M2M + 450k L2L, P_in, P_out iid U{4..24}, sources "
+                                   "gathered from 65 536 expansions per kind, distinct targets, FP64 storage at "
+                                   "stride 600", "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{world}"},
+            "plan": {"segments": len(segs), "launches_per_step": launches, "cuda_graph": True},
+            "plan_plain_fp64": rate(ms_plan_plain),
+            "unsorted_one_launch_per_op": {"split": rate(ms_unsorted), "plain_fp64": rate(ms_unsorted_plain)},
+            "per_order_pair_launches": {"split": rate(ms_pairs), "plain_fp64": rate(ms_pairs_plain),
+                                        "launches_per_step": len(groups)},
+            "clocks": clk, "gpu_launches": launches}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -248,6 +386,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    if args.workload == "mixed":
+        return run_mixed(args)
     op, P, N, nq = WORKLOADS[args.workload]
     world, rank, local = dist_init(args)
     config = {"workload": f"{op.upper()} P={P} (reference order: degrees 0..{P - 1}), {N} translations per GPU, "

@@ -150,6 +150,32 @@ int sfmm_set_group(sfmm_context *ctx, int precision, size_t order_bound, int gro
 int sfmm_tune(sfmm_context *ctx, int op, int precision, size_t order_bound, size_t n, int *group,
               double *rate);
 
+/* Execution plans.  A plan is an ordered list of device batches (stages)
+ * that runs many times with the same orders and indices: one FMM pass, a
+ * mixed-order workload.  sfmm_plan_finalize reads each stage's orders,
+ * sorts its translations by order bound max(p_in, p_out) (then by the
+ * pair), splits the sorted stage into segments of one order bound, and
+ * records one kernel launch per segment into a CUDA graph; the segments of a
+ * stage run on concurrent graph branches, the stages in order (a stage sees
+ * the results of the ones before it).  sfmm_plan_run replays the graph on
+ * the context's stream (asynchronous).  The stage arrays are device
+ * pointers that must stay valid, with unchanged orders and indices, while
+ * the plan exists; expansions and shifts may change between runs.  Because
+ * the segments of a stage run concurrently, a stage whose targets repeat
+ * must pass SFMM_TARGETS_REPEAT.  sfmm_plan_segments reports the segments
+ * (order bound and size, all stages in order; returns their number). */
+typedef struct sfmm_plan sfmm_plan;
+int sfmm_plan_create(sfmm_context *ctx, sfmm_plan **plan);
+int sfmm_plan_add(sfmm_plan *plan, int op, int precision, size_t n,
+                  const void *src, size_t src_stride, size_t src_count, const uint32_t *src_index,
+                  void *dst, size_t dst_stride, size_t dst_count, const uint32_t *dst_index,
+                  const uint32_t *p_in, const uint32_t *p_out, const double *shift, int flags);
+int sfmm_plan_finalize(sfmm_plan *plan);
+int sfmm_plan_run(sfmm_plan *plan);
+size_t sfmm_plan_launches(const sfmm_plan *plan);
+size_t sfmm_plan_segments(const sfmm_plan *plan, int *bounds, size_t *counts, size_t cap);
+void sfmm_plan_destroy(sfmm_plan *plan);
+
 /* Bucket a device batch by (p_in, p_out): writes a permutation of 0..n-1 into
  * `order` (device, n entries) so that translations of equal order pairs are
  * contiguous.  Uses ctx scratch; asynchronous. */

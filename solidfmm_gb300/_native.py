@@ -27,7 +27,8 @@ EXPORTS = [
     "sfmm_set_stream", "sfmm_translate_device", "sfmm_device_status", "sfmm_translate_host_packed",
     "sfmm_translate_host", "sfmm_bucket_by_order", "sfmm_p2x_device", "sfmm_launch_count",
     "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak", "sfmm_bucket_by_order_noalloc",
-    "sfmm_set_group", "sfmm_tune",
+    "sfmm_set_group", "sfmm_tune", "sfmm_plan_create", "sfmm_plan_add", "sfmm_plan_finalize", "sfmm_plan_run",
+    "sfmm_plan_launches", "sfmm_plan_segments", "sfmm_plan_destroy",
 ]
 
 
@@ -81,6 +82,17 @@ def load():
     L.sfmm_measure_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.sfmm_measure_imad_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.sfmm_bucket_by_order_noalloc.argtypes = [sz, u32p, u32p, u32p, sz, vp]
+    L.sfmm_plan_create.argtypes = [vp, C.POINTER(vp)]
+    L.sfmm_plan_add.argtypes = [vp, C.c_int, C.c_int, sz, vp, sz, sz, u32p, vp, sz, sz, u32p, u32p, u32p, dp,
+                                C.c_int]
+    L.sfmm_plan_finalize.argtypes = [vp]
+    L.sfmm_plan_run.argtypes = [vp]
+    L.sfmm_plan_launches.argtypes = [vp]
+    L.sfmm_plan_launches.restype = sz
+    L.sfmm_plan_segments.argtypes = [vp, vp, vp, sz]
+    L.sfmm_plan_segments.restype = sz
+    L.sfmm_plan_destroy.argtypes = [vp]
+    L.sfmm_plan_destroy.restype = None
     _lib = L
     return L
 
@@ -200,3 +212,55 @@ class Context:
     def p2x(self, kind, nexp, nq, charge, pos, centre, out, out_stride):
         self._check(self.L.sfmm_p2x_device(self.h, kind, nexp, nq, _ptr(charge), _ptr(pos), _ptr(centre),
                                            _ptr(out), out_stride))
+
+
+class Plan:
+    """An execution plan (sfmm_plan_*): stages of device batches recorded
+    once into a CUDA graph, sorted and segmented by order, replayed by run().
+    Tensors passed to add() are kept alive by the plan."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.L = ctx.L
+        h = C.c_void_p()
+        ctx._check(self.L.sfmm_plan_create(ctx.h, C.byref(h)))
+        self.h = h
+        self._keep = []
+
+    def add(self, op, precision, n, src, src_stride, src_count, dst, dst_stride, dst_count, p_in, p_out, shift,
+            src_index=None, dst_index=None, repeat=False):
+        self._keep += [src, dst, p_in, p_out, shift, src_index, dst_index]
+        self.ctx._check(self.L.sfmm_plan_add(
+            self.h, OPS.get(op, op), precision, n, _ptr(src), src_stride, src_count, _ptr(src_index), _ptr(dst),
+            dst_stride, dst_count, _ptr(dst_index), _ptr(p_in), _ptr(p_out), _ptr(shift),
+            TARGETS_REPEAT if repeat else TARGETS_UNIQUE))
+        return self
+
+    def finalize(self):
+        self.ctx._check(self.L.sfmm_plan_finalize(self.h))
+        return self
+
+    def run(self):
+        self.ctx._check(self.L.sfmm_plan_run(self.h))
+
+    @property
+    def launches(self) -> int:
+        return self.L.sfmm_plan_launches(self.h)
+
+    def segments(self):
+        k = self.L.sfmm_plan_segments(self.h, None, None, 0)
+        b = (C.c_int * max(k, 1))()
+        n = (C.c_size_t * max(k, 1))()
+        self.L.sfmm_plan_segments(self.h, b, n, k)
+        return [(b[i], n[i]) for i in range(k)]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sfmm_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -19,86 +19,14 @@
 #include <unordered_map>
 #include <vector>
 
+#include "sfmm_context.hpp"
 #include "sfmm_launch.hpp"
-#include "sfmm_tables.hpp"
 #include "sfmm_params.hpp"
+#include "sfmm_tables.hpp"
 
 using namespace sfmm;
 
-namespace {
-
-struct DevTables {
-    void *W = nullptr, *ein_M = nullptr, *ein_L = nullptr, *eout_L = nullptr, *eout_M = nullptr;
-    void *H[3] = {nullptr, nullptr, nullptr};
-    void *Wq = nullptr;  // Q1.30 swap matrices (fixed-point variant only)
-    bool ready = false;
-};
-
-struct DevBuf {
-    void *p = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t b)
-    {
-        if (b <= bytes) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMalloc(&p, b);
-        if (e == cudaSuccess) bytes = b;
-        return e;
-    }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-};
-
-struct HostBuf {
-    void *p = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t b)
-    {
-        if (b <= bytes) return cudaSuccess;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMallocHost(&p, b);
-        if (e == cudaSuccess) bytes = b;
-        return e;
-    }
-    void release()
-    {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-    }
-};
-
-}  // namespace
-
-struct sfmm_context {
-    int dtype = SFMM_F64;
-    int P = 0;
-    int device = 0;
-    int num_sms = 0;
-    cudaStream_t stream = nullptr;
-    HostTables host;
-    DevTables tab[4];  // indexed by Arith
-    std::string err;
-    uint64_t launches = 0;
-    std::mutex mtx;  // serialises host-path calls (one translator object, one stream)
-    int *d_status = nullptr;  // device error word of the translation kernels
-    // host-path staging (three pipeline slots for the packed host call)
-    DevBuf d_src[3], d_dst[3], d_meta[3], d_shift[3], d_work;
-    HostBuf h_src, h_dst, h_meta, h_shift;
-    cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
-    std::map<std::pair<int, int>, LaunchShape> shapes;  // (arith, order bound) -> launch shape
-    int *d_woff = nullptr, *d_hoff = nullptr;            // table offsets (shared by all arithmetics)
-};
-
-namespace {
+namespace sfmm {
 
 int fail(sfmm_context *c, int st, const char *fmt, ...)
 {
@@ -215,24 +143,34 @@ Arith resolve_arith(Arith a, int op, int Pbound)
     return a;
 }
 
+int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound)
+{
+    a = resolve_arith(a, op, Pbound);
+    if (Pbound < 1) Pbound = 1;
+    int st = ensure_tables(c, a);
+    if (st) return st;
+    const auto key = std::make_pair((int)a, Pbound);
+    auto it = c->shapes.find(key);
+    if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound, default_group(a, Pbound))).first;
+    if (it->second.acc == 0)
+        return fail(c, SFMM_UNSUPPORTED, "order %d exceeds the GPU kernels' limit %d", Pbound, kMaxKernelOrder);
+    if (a != Arith::F64 && Pbound > kMaxFloatOrder)
+        return fail(c, SFMM_UNSUPPORTED, "order %d exceeds %d, the limit of FP32-range arithmetic", Pbound, kMaxFloatOrder);
+    return SFMM_OK;
+}
+
 // The launch itself: validated arguments, device pointers.
 int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound, long long n, const void *src,
               long long sstride, long long nsrc, const uint32_t *sidx, void *dst, long long dstride, long long ndst,
               const uint32_t *tidx, const uint32_t *pin, const uint32_t *pout, const double *shift,
-              const uint32_t *perm, int flags)
+              const uint32_t *perm, int flags, long long nidx)
 {
     if (n == 0) return SFMM_OK;
     a = resolve_arith(a, op, Pbound);
-    int st = ensure_tables(c, a);
-    if (st) return st;
     if (Pbound < 1) Pbound = 1;
-    auto key = std::make_pair((int)a, Pbound);
-    auto it = c->shapes.find(key);
-    if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound, default_group(a, Pbound))).first;
-    LaunchShape s = it->second;
-    if (s.acc == 0) return fail(c, SFMM_UNSUPPORTED, "order %d exceeds the GPU kernels' limit %d", Pbound, kMaxKernelOrder);
-    if (a != Arith::F64 && Pbound > kMaxFloatOrder)
-        return fail(c, SFMM_UNSUPPORTED, "order %d exceeds %d, the limit of FP32-range arithmetic", Pbound, kMaxFloatOrder);
+    int st = prepare_launch(c, op, a, Pbound);
+    if (st) return st;
+    const LaunchShape s = c->shapes.find(std::make_pair((int)a, Pbound))->second;
     const DevTables &t = c->tab[(int)a];
     KParams p{};
     p.op = op;
@@ -252,6 +190,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.pout = pout;
     p.shift = shift;
     p.perm = perm;
+    p.nidx = nidx < 0 ? n : nidx;
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
     p.W = t.W;
     p.Wq = static_cast<const int *>(t.Wq);
@@ -264,7 +203,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.spad = s.spad;
     p.TS = s.TS;
     long long tiles = (n + s.TS - 1) / s.TS;
-    long long grid = (long long)c->num_sms * translate_blocks_per_sm(a, s);
+    long long grid = (long long)c->num_sms * s.blocks_per_sm;
     if (grid > tiles) grid = tiles;
     cudaError_t e = launch_translate(a, p, s, (int)grid, stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "translation kernel launch");
@@ -272,7 +211,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     return SFMM_OK;
 }
 
-}  // namespace
+}  // namespace sfmm
 
 namespace sfmm {
 
@@ -329,7 +268,8 @@ LaunchShape best_shape(Arith a, int P, int G)
     for (int ts = 256 / G; ts >= 32 / G; ts -= 32 / G) {
         LaunchShape s = translate_shape(a, P, G, ts);
         if (!s.acc) continue;
-        long th = (long)translate_blocks_per_sm(a, s) * s.threads;
+        s.blocks_per_sm = translate_blocks_per_sm(a, s);
+        long th = (long)s.blocks_per_sm * s.threads;
         if (th > best_threads) {
             best_threads = th;
             best = s;

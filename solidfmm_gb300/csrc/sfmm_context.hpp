@@ -1,0 +1,111 @@
+// Context internals shared by the C ABI (sfmm_capi.cpp) and the execution
+// plans (sfmm_plan.cpp).  Not part of the public interface.
+#pragma once
+
+#include "sfmm.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "sfmm_launch.hpp"
+#include "sfmm_tables.hpp"
+
+namespace sfmm {
+
+struct DevTables {
+    void *W = nullptr, *ein_M = nullptr, *ein_L = nullptr, *eout_L = nullptr, *eout_M = nullptr;
+    void *H[3] = {nullptr, nullptr, nullptr};
+    void *Wq = nullptr;  // Q1.30 swap matrices (fixed-point variant only)
+    bool ready = false;
+};
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b)
+    {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+struct HostBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b)
+    {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMallocHost(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+}  // namespace sfmm
+
+struct sfmm_context {
+    int dtype = SFMM_F64;
+    int P = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    sfmm::HostTables host;
+    sfmm::DevTables tab[4];  // indexed by Arith
+    std::string err;
+    uint64_t launches = 0;
+    std::mutex mtx;  // serialises host-path calls (one translator object, one stream)
+    int *d_status = nullptr;  // device error word of the translation kernels
+    // host-path staging (three pipeline slots for the packed host call)
+    sfmm::DevBuf d_src[3], d_dst[3], d_meta[3], d_shift[3], d_work;
+    sfmm::HostBuf h_src, h_dst, h_meta, h_shift;
+    cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
+    std::map<std::pair<int, int>, sfmm::LaunchShape> shapes;  // (arith, order bound) -> launch shape
+    int *d_woff = nullptr, *d_hoff = nullptr;            // table offsets (shared by all arithmetics)
+};
+
+namespace sfmm {
+
+// record an error on the context and return the status
+int fail(sfmm_context *c, int st, const char *fmt, ...);
+int cuda_fail(sfmm_context *c, cudaError_t e, const char *what);
+// arithmetic of a precision mode on this context
+int arith_of(sfmm_context *c, int precision, Arith *out);
+// upload the arithmetic's tables once
+int ensure_tables(sfmm_context *c, Arith a);
+// tables and launch shape of (arithmetic, order bound) for op, so that a
+// launch makes no allocation (plans call this before a graph capture)
+int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound);
+// one validated translation launch on device pointers (translation i of the
+// batch is perm[i] when perm is given)
+int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound, long long n, const void *src,
+              long long sstride, long long nsrc, const uint32_t *sidx, void *dst, long long dstride, long long ndst,
+              const uint32_t *tidx, const uint32_t *pin, const uint32_t *pout, const double *shift,
+              const uint32_t *perm, int flags, long long nidx = -1);
+
+}  // namespace sfmm

@@ -11,17 +11,13 @@
 
 namespace sfmm {
 
+// Launch shapes come from best_shape, whose occupancy query (below) has set
+// the kernel's shared-memory limit on the current device, so a launch (also
+// inside a CUDA graph capture) makes no other runtime call.
 template <class A, int G, int ACC, bool FIX>
 static cudaError_t launch_inst(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
-    static bool attr_set = false;
-    auto kern = k_translate<A, G, ACC, FIX>;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    kern<<<grid, s.threads, s.smem, st>>>(p);
+    k_translate<A, G, ACC, FIX><<<grid, s.threads, s.smem, st>>>(p);
     return cudaGetLastError();
 }
 

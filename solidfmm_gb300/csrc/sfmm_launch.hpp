@@ -28,6 +28,7 @@ struct LaunchShape {
     int spad = 0;      // buffer elements per translation
     size_t smem = 0;   // dynamic shared memory bytes
     int threads = 0;   // G * TS
+    int blocks_per_sm = 0;  // resident CTAs per SM (occupancy of this shape)
 };
 
 LaunchShape translate_shape(Arith a, int P, int G, int ts);

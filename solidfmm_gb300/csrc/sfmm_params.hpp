@@ -24,6 +24,7 @@ struct KParams {
     const uint32_t *pout;
     const double *shift;
     const uint32_t *perm;
+    long long nidx;     // entries of pin/pout/shift/sidx/tidx (perm values index these)
     int atomic;
     const void *W;      // arith-typed swap matrices (padded, see sfmm_tables.hpp)
     const int *Wq;      // swap matrices in Q1.30 (fixed-point variant), same layout as W

@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         uint32_t t = 0, si = 0, ti = 0;
         if (valid) t = p.perm ? p.perm[i] : (uint32_t)i;
         int pin = 0, pout = 0;
-        if (valid && t < p.n) {
+        if (valid && t < p.nidx) {
             si = p.sidx ? p.sidx[t] : t;
             ti = p.tidx ? p.tidx[t] : t;
             pin = (int)p.pin[t];
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         }
         // malformed entries (the unchecked API's undefined behaviour) are
         // skipped and reported instead of touching memory out of bounds
-        if (valid && (t >= p.n || si >= p.nsrc || ti >= p.ndst || pin > P || pout > P || pin < 0 || pout < 0)) {
+        if (valid && (t >= p.nidx || si >= p.nsrc || ti >= p.ndst || pin > P || pout > P || pin < 0 || pout < 0)) {
             if (q == 0) atomicOr(p.status, 1);
             valid = false;
             pin = pout = 0;
