@@ -205,6 +205,17 @@ int sfmm_bucket_by_order_noalloc(size_t n, const uint32_t *p_in, const uint32_t 
  *   out[j] += sum_{k<nq} charge[j*nq+k] * R(pos[j*nq+k] - centre[j])   (kind 0)
  *   out[j] += sum_{k<nq} charge[j*nq+k] * S(pos[j*nq+k] - centre[j])   (kind 1)
  * FP64 arithmetic; out has the context's data type and order P. */
+/* L2P / M2P on the device: for point j with expansion b = box[j] (box NULL:
+ * b = j; nexp expansions addressable at `stride` reals, centres FP64),
+ *   potential[j] += dot(E[b], R(pos[j] - centre[b]))    (kind 0, local)
+ *   potential[j] += dot(E[b], S(pos[j] - centre[b]))    (kind 1, multipole)
+ * with dot the reference's solid dot product (solid.cpp:41-66).  For kind 0
+ * a non-NULL gradient (3 per point) receives += grad phi(pos[j]) as well.
+ * FP64 arithmetic; box indices are not range-checked (device data). */
+int sfmm_eval_device(sfmm_context *ctx, int kind, size_t npts, const double *pos, const uint32_t *box,
+                     const void *E, size_t stride, size_t nexp, const double *centre, double *potential,
+                     double *gradient);
+
 int sfmm_p2x_device(sfmm_context *ctx, int kind, size_t nexp, size_t nq, const double *charge,
                     const double *pos, const double *centre, void *out, size_t out_stride);
 

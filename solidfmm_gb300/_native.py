@@ -28,7 +28,7 @@ EXPORTS = [
     "sfmm_translate_host", "sfmm_bucket_by_order", "sfmm_p2x_device", "sfmm_launch_count",
     "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak", "sfmm_bucket_by_order_noalloc",
     "sfmm_set_group", "sfmm_tune", "sfmm_plan_create", "sfmm_plan_add", "sfmm_plan_finalize", "sfmm_plan_run",
-    "sfmm_plan_launches", "sfmm_plan_segments", "sfmm_plan_destroy",
+    "sfmm_plan_launches", "sfmm_plan_segments", "sfmm_plan_destroy", "sfmm_eval_device",
 ]
 
 
@@ -82,6 +82,7 @@ def load():
     L.sfmm_measure_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.sfmm_measure_imad_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.sfmm_bucket_by_order_noalloc.argtypes = [sz, u32p, u32p, u32p, sz, vp]
+    L.sfmm_eval_device.argtypes = [vp, C.c_int, sz, dp, u32p, vp, sz, sz, dp, dp, dp]
     L.sfmm_plan_create.argtypes = [vp, C.POINTER(vp)]
     L.sfmm_plan_add.argtypes = [vp, C.c_int, C.c_int, sz, vp, sz, sz, u32p, vp, sz, sz, u32p, u32p, u32p, dp,
                                 C.c_int]
@@ -208,6 +209,12 @@ class Context:
 
     def bucket(self, n, p_in, p_out, order):
         self._check(self.L.sfmm_bucket_by_order(self.h, n, _ptr(p_in), _ptr(p_out), _ptr(order)))
+
+    def evaluate(self, kind, npts, pos, E, stride, nexp, centre, potential, gradient=None, box=None):
+        """L2P (kind 0) / M2P (kind 1): potential[j] (+ gradient) += the
+        expansion's field at pos[j] (sfmm_eval_device)."""
+        self._check(self.L.sfmm_eval_device(self.h, kind, npts, _ptr(pos), _ptr(box), _ptr(E), stride, nexp,
+                                            _ptr(centre), _ptr(potential), _ptr(gradient)))
 
     def p2x(self, kind, nexp, nq, charge, pos, centre, out, out_stride):
         self._check(self.L.sfmm_p2x_device(self.h, kind, nexp, nq, _ptr(charge), _ptr(pos), _ptr(centre),

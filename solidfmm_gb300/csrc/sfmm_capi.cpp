@@ -599,6 +599,25 @@ int sfmm_p2x_device(sfmm_context *c, int kind, size_t nexp, size_t nq, const dou
     return SFMM_OK;
 }
 
+int sfmm_eval_device(sfmm_context *c, int kind, size_t npts, const double *pos, const uint32_t *box,
+                     const void *E, size_t stride, size_t nexp, const double *centre, double *potential,
+                     double *gradient)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    if (kind != 0 && kind != 1) return fail(c, SFMM_INVALID_ARG, "kind must be 0 (L2P) or 1 (M2P)");
+    if (npts == 0) return SFMM_OK;
+    if (!pos || !E || !centre || !potential) return fail(c, SFMM_INVALID_ARG, "null device pointer");
+    if (stride < (size_t)c->P * (c->P + 1)) return fail(c, SFMM_INVALID_ARG, "stride smaller than P(P+1)");
+    if (gradient && kind != 0) return fail(c, SFMM_UNSUPPORTED, "gradients are evaluated for local expansions");
+    if (!box && nexp < npts) return fail(c, SFMM_INVALID_ARG, "fewer expansions than points without a box index");
+    cudaSetDevice(c->device);
+    cudaError_t e = launch_eval(c->dtype == SFMM_F64, kind, c->P, (long long)npts, pos, box, E, (long long)stride,
+                                centre, potential, gradient, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "L2P/M2P kernel");
+    c->launches++;
+    return SFMM_OK;
+}
+
 int sfmm_translate_host_packed(sfmm_context *c, int op, int precision, size_t n, const void *src,
                                size_t src_stride, size_t src_count, const uint32_t *src_index, void *dst,
                                size_t dst_stride, size_t dst_count, const uint32_t *dst_index, const uint32_t *p_in,

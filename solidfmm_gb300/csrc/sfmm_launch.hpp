@@ -43,6 +43,11 @@ int translate_blocks_per_sm(Arith a, const LaunchShape &s);
 cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const double *q,
                        const double *pos, const double *centre, void *out, long long stride, cudaStream_t st);
 
+// L2P / M2P evaluation (sfmm_p2x.cu)
+cudaError_t launch_eval(bool f64, int kind, int P, long long npts, const double *pos, const uint32_t *box,
+                        const void *E, long long stride, const double *centre, double *pot, double *grad,
+                        cudaStream_t st);
+
 // bucketing by order pair (sfmm_p2x.cu)
 cudaError_t launch_bucket(long long n, const uint32_t *pin, const uint32_t *pout, uint32_t *order,
                           uint32_t *work, int P, cudaStream_t st);

@@ -116,6 +116,133 @@ cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, 
     return cudaGetLastError();
 }
 
+// ---- evaluation (L2P / M2P) ----
+//
+// phi(x) = dot(E, R(x - c)) for a local expansion (kind 0) or
+// dot(E, S(x - c)) for a multipole expansion (kind 1), the reference's
+// solid dot product (solid.cpp:41-66): sum over n, m >= 0 of re*re + im*im,
+// weighted 2 for m > 0.  The harmonics are produced column by column as in
+// P2M/P2L and consumed at once, so a thread keeps no expansion-sized state.
+// The gradient of a local expansion uses (d/dx - i d/dy) R_n^m = R_{n-1}^{m-1},
+// (d/dx + i d/dy) R_n^m = -R_{n-1}^{m+1} and d/dz R_n^m = R_{n-1}^m: each
+// R_k^v produced pairs with the degree-(k+1) coefficients v-1, v, v+1.
+template <class In>
+__global__ void k_eval(int kind, int P, long long npts, const double *__restrict__ pos,
+                       const uint32_t *__restrict__ box, const In *__restrict__ E, long long stride,
+                       const double *__restrict__ centre, double *pot, double *grad)
+{
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= npts) return;
+    const long long b = box ? (long long)box[j] : j;
+    const In *e = E + b * stride;
+    const double x = pos[3 * j] - centre[3 * b], y = pos[3 * j + 1] - centre[3 * b + 1],
+                 z = pos[3 * j + 2] - centre[3 * b + 2];
+    const double r2 = x * x + y * y + z * z;
+    auto re = [&](int n, int m) { return (double)e[n * (n + 1) + m]; };
+    auto im = [&](int n, int m) { return (double)e[(n + 1) * (n + 1) + m]; };
+    double phi = 0, gx = 0, gy = 0, gz = 0;
+    const bool want_grad = grad != nullptr && kind == 0;
+    if (kind == 0) {
+        double dr = 1.0, di = 0.0;  // R(m,m)
+        for (int m = 0; m < P; ++m) {
+            if (m > 0) {
+                const double f = 1.0 / (2.0 * m);
+                const double nr = (dr * x - di * y) * f, ni = (dr * y + di * x) * f;
+                dr = nr;
+                di = ni;
+            }
+            const double w = m ? 2.0 : 1.0;
+            double ar = dr, ai = di, br = 0.0, bi = 0.0;
+            for (int n = m; n < P; ++n) {
+                double cr = ar, ci = ai;  // R(n,m)
+                if (n == m + 1) {
+                    cr = z * ar;
+                    ci = z * ai;
+                } else if (n > m + 1) {
+                    const double f = 1.0 / ((double)(n + m) * (double)(n - m));
+                    cr = (ar * z * (2 * n - 1) - r2 * br) * f;
+                    ci = (ai * z * (2 * n - 1) - r2 * bi) * f;
+                }
+                phi += w * (re(n, m) * cr + im(n, m) * ci);
+                if (want_grad && n + 1 < P) {
+                    const int k1 = n + 1;
+                    gz += w * (re(k1, m) * cr + im(k1, m) * ci);
+                    if (m == 0) {
+                        gx += cr * re(k1, 1);
+                        gy += cr * im(k1, 1);
+                    } else {
+                        // conj(R) (L^{m+1} - L^{m-1}) and conj(R) (L^{m-1} + L^{m+1})
+                        const double xr = re(k1, m + 1) - re(k1, m - 1), xi = im(k1, m + 1) - im(k1, m - 1);
+                        const double yr = re(k1, m - 1) + re(k1, m + 1), yi = im(k1, m - 1) + im(k1, m + 1);
+                        gx += cr * xr + ci * xi;
+                        gy += cr * yi - ci * yr;
+                    }
+                }
+                if (n > m) {
+                    br = ar;
+                    bi = ai;
+                    ar = cr;
+                    ai = ci;
+                }
+            }
+        }
+    } else {
+        const double r2inv = 1.0 / r2;
+        double dr = sqrt(r2inv), di = 0.0;  // S(m,m)
+        for (int m = 0; m < P; ++m) {
+            if (m > 0) {
+                const double f = (2.0 * m - 1.0) * r2inv;
+                const double nr = (dr * x - di * y) * f, ni = (dr * y + di * x) * f;
+                dr = nr;
+                di = ni;
+            }
+            const double w = m ? 2.0 : 1.0;
+            double ar = dr, ai = di, br = 0.0, bi = 0.0;
+            for (int n = m; n < P; ++n) {
+                double cr = ar, ci = ai;
+                if (n == m + 1) {
+                    const double f = (2.0 * m + 1.0) * z * r2inv;
+                    cr = f * ar;
+                    ci = f * ai;
+                } else if (n > m + 1) {
+                    const double c2 = (double)(n + m - 1) * (double)(n - m - 1);
+                    cr = (ar * z * (2 * n - 1) - c2 * br) * r2inv;
+                    ci = (ai * z * (2 * n - 1) - c2 * bi) * r2inv;
+                }
+                phi += w * (re(n, m) * cr + im(n, m) * ci);
+                if (n > m) {
+                    br = ar;
+                    bi = ai;
+                    ar = cr;
+                    ai = ci;
+                }
+            }
+        }
+    }
+    pot[j] += phi;
+    if (want_grad) {
+        grad[3 * j] += gx;
+        grad[3 * j + 1] += gy;
+        grad[3 * j + 2] += gz;
+    }
+}
+
+cudaError_t launch_eval(bool f64, int kind, int P, long long npts, const double *pos, const uint32_t *box,
+                        const void *E, long long stride, const double *centre, double *pot, double *grad,
+                        cudaStream_t st)
+{
+    if (npts == 0) return cudaSuccess;
+    const int tb = 128;
+    const long long grid = (npts + tb - 1) / tb;
+    if (f64)
+        k_eval<double><<<(unsigned)grid, tb, 0, st>>>(kind, P, npts, pos, box, (const double *)E, stride, centre,
+                                                       pot, grad);
+    else
+        k_eval<float><<<(unsigned)grid, tb, 0, st>>>(kind, P, npts, pos, box, (const float *)E, stride, centre,
+                                                      pot, grad);
+    return cudaGetLastError();
+}
+
 // ---- bucketing by (p_in, p_out) ----
 
 __global__ void k_bucket_count(long long n, const uint32_t *pin, const uint32_t *pout, uint32_t *cnt, int K)

@@ -1,0 +1,108 @@
+"""GPU evaluation of expansions (sfmm_eval_device): L2P and M2P potentials
+against the oracle's dot(E, R/S(x - c)), L2P gradients against central
+differences of the oracle potential, and the physics of P2M -> M2L -> L2P
+against direct summation."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _pot(oracle, kind, E, P, pts, centre):
+    h = "R" if kind == 0 else "S"
+    return np.array([oracle.dot(E, P, oracle.harmonic(h, P, *(p - centre)), P) for p in pts])
+
+
+@pytest.mark.parametrize("P", [1, 6, 12, 20])
+@pytest.mark.parametrize("kind", [0, 1], ids=["l2p", "m2p"])
+def test_eval_matches_oracle(native, oracle, kind, P):
+    import torch
+
+    rng = np.random.default_rng(P + 10 * kind)
+    nexp, per = 5, 40
+    q = rng.choice([-1.0, 1.0], size=(nexp, 16))
+    d = rng.normal(size=(nexp, 16, 3))
+    src = d / np.linalg.norm(d, axis=2, keepdims=True) * (0.4 * rng.random((nexp, 16, 1)))
+    if kind == 0:  # local expansions of far clouds
+        src = src + np.array([3.0, -1.0, 2.0])
+    centres = rng.normal(size=(nexp, 3)) * 0.1
+    E = oracle.p2m(P, q, src + centres[:, None, :], centres, singular=(kind == 0))
+    # points: near the centre for locals, far away for multipoles
+    u = rng.normal(size=(nexp * per, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    rad = 0.45 * rng.random((nexp * per, 1)) if kind == 0 else 2.5 + rng.random((nexp * per, 1))
+    box = np.repeat(np.arange(nexp), per).astype(np.uint32)
+    pts = u * rad + centres[box]
+    ref = np.concatenate([_pot(oracle, kind, E[b], P, pts[box == b], centres[b]) for b in range(nexp)])
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    pot = torch.zeros(len(pts), dtype=torch.float64, device=dev)
+    S = P * (P + 1)
+    ctx.evaluate(kind, len(pts), torch.as_tensor(pts, device=dev), torch.as_tensor(E, device=dev), S, nexp,
+                 torch.as_tensor(centres, device=dev), pot, box=torch.as_tensor(box.astype(np.int32), device=dev))
+    torch.cuda.synchronize()
+    got = pot.cpu().numpy()
+    assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref)) + 1e-300
+
+
+def test_l2p_gradient_is_derivative(native, oracle):
+    import torch
+
+    P = 12
+    rng = np.random.default_rng(3)
+    q = rng.choice([-1.0, 1.0], size=(1, 24))
+    d = rng.normal(size=(1, 24, 3))
+    src = d / np.linalg.norm(d, axis=2, keepdims=True) * 0.4 + np.array([2.5, 1.0, -1.5])
+    L = oracle.p2m(P, q, src, np.zeros((1, 3)), singular=True)
+    pts = rng.normal(size=(50, 3)) * 0.2
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    pot = torch.zeros(50, dtype=torch.float64, device=dev)
+    grad = torch.zeros(50, 3, dtype=torch.float64, device=dev)
+    ctx.evaluate(0, 50, torch.as_tensor(pts, device=dev), torch.as_tensor(L, device=dev), P * (P + 1), 1,
+                 torch.zeros(1, 3, dtype=torch.float64, device=dev), pot, gradient=grad,
+                 box=torch.zeros(50, dtype=torch.int32, device=dev))
+    torch.cuda.synchronize()
+    g = grad.cpu().numpy()
+    h = 1e-5
+    fd = np.zeros_like(g)
+    for a in range(3):
+        e = np.zeros(3)
+        e[a] = h
+        fd[:, a] = (_pot(oracle, 0, L[0], P, pts + e, np.zeros(3)) - _pot(oracle, 0, L[0], P, pts - e, np.zeros(3))) / (2 * h)
+    assert np.max(np.abs(g - fd)) <= 1e-8 * np.max(np.abs(fd))
+
+
+def test_p2m_m2l_l2p_physics(native):
+    """Charges in a ball of radius 0.5, targets near a centre at distance 4.1:
+    P2M -> M2L -> L2P (split precision) reproduces the direct potential and
+    field to the truncation error of order 16."""
+    import torch
+
+    rng = np.random.default_rng(11)
+    P = 16
+    dev = torch.device("cuda", 0)
+    d = rng.normal(size=(64, 3))
+    ys = d / np.linalg.norm(d, axis=1, keepdims=True) * (0.5 * rng.random((64, 1)) ** (1 / 3))
+    qs = rng.choice([-1.0, 1.0], size=64)
+    ctr = np.array([[2.0, -2.0, 3.0]])
+    xs = ctr + rng.normal(size=(100, 3)) * 0.1
+    ctx = native.Context(P, "f64")
+    S = P * (P + 1)
+    M = torch.zeros(1, S, dtype=torch.float64, device=dev)
+    ctx.p2x(0, 1, 64, torch.as_tensor(qs[None, :], device=dev), torch.as_tensor(ys[None], device=dev),
+            torch.zeros(1, 3, dtype=torch.float64, device=dev), M, S)
+    L = torch.zeros(1, S, dtype=torch.float64, device=dev)
+    one = torch.full((1,), P, dtype=torch.int32, device=dev)
+    ctx.translate_device("m2l", 1, 1, M, S, 1, L, S, 1, one, one, torch.as_tensor(ctr, device=dev))
+    pot = torch.zeros(100, dtype=torch.float64, device=dev)
+    grad = torch.zeros(100, 3, dtype=torch.float64, device=dev)
+    ctx.evaluate(0, 100, torch.as_tensor(xs, device=dev), L, S, 1, torch.as_tensor(ctr, device=dev), pot,
+                 gradient=grad, box=torch.zeros(100, dtype=torch.int32, device=dev))
+    torch.cuda.synchronize()
+    diff = xs[:, None, :] - ys[None, :, :]
+    r = np.linalg.norm(diff, axis=2)
+    phi = (qs / r).sum(1)
+    field = -(qs[None, :, None] * diff / r[..., None] ** 3).sum(1)  # grad of sum q/r
+    assert np.max(np.abs(pot.cpu().numpy() - phi)) < 1e-7 * np.max(np.abs(phi))
+    assert np.max(np.abs(grad.cpu().numpy() - field)) < 1e-6 * np.max(np.abs(field))
