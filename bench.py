@@ -44,6 +44,9 @@ WORKLOADS = {
     "l2l20": ("l2l", 20, 1_000_000, 128),
     # 1.5e6 translations, 40% M2L / 30% M2M / 30% L2L, orders U{4..24}
     "mixed": ("mixed", 24, 1_500_000, 64),
+    # one FMM pass: uniform octree of depth 5 (32 768 leaves) on the unit cube,
+    # 32 charges U[-1, 1] per leaf, P=12
+    "fmm": ("fmm", 12, 32768, 32),
 }
 
 METRIC = "M2L translations/s at P=16, chosen vs plain FP64 GPU at equal rel. error; %roofline"
@@ -376,6 +379,122 @@ def run_mixed(args):
     print(json.dumps(line))
 
 
+FMM_METRIC = "FMM pass time (P2M + M2M + M2L + L2L), uniform octree depth 5, P=12, 32 charges per leaf"
+
+
+def run_fmm(args):
+    """One FMM pass on a depth-5 uniform octree at P=12 (solidfmm_gb300.fmm):
+    P2M at the leaves, M2M to level 2, M2L over the interaction lists of
+    levels 2..5, L2L to the leaves, in one execution plan.  The leaf locals
+    are checked against the oracle's CPU pass (FP64 rotation method), whose
+    time is the CPU baseline, and the potential (L2P + near-field direct
+    sums) against direct summation at 2 000 sampled particles."""
+    import torch
+    import solidfmm_gb300 as sf
+    from solidfmm_gb300 import build as _b
+    from solidfmm_gb300 import fmm
+
+    world, rank, local = dist_init(args)
+    _b.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    depth, P, per = 5, 12, 32
+    ctx = sf.Context(P, "f64", device=local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    q, pos = fmm.random_particles(depth, per, 900 + rank, dev)
+    f = fmm.UniformFMM(ctx, depth, sf.SPLIT, dev)
+    fp = fmm.UniformFMM(ctx, depth, sf.PLAIN, dev)
+    counts = f.translations
+    ntr = sum(counts.values())
+
+    def timed(obj, steps, warmup):
+        for _ in range(warmup):
+            obj.run(q, pos)
+        torch.cuda.synchronize()
+        barrier(world)
+        l0 = ctx.launches
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            obj.run(q, pos)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        return allmax(world, e0.elapsed_time(e1) / steps, dev), (ctx.launches - l0) // max(steps, 1)
+
+    clocks = Clocks(local)
+    clocks.start()
+    ms, launches = timed(f, args.steps, args.warmup)
+    clk = clocks.stop()
+    ms_plain, _ = timed(fp, max(2, args.steps // 2), 1)
+    if rank != 0:
+        return
+    # physics: potential at sampled particles, far field (L2P) + near field vs direct sum
+    f.run(q, pos)
+    nleaf = 8 ** depth
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    samp = torch.randint(0, nleaf * per, (2000,), device=dev, generator=g)
+    pts = pos.reshape(-1, 3)[samp].contiguous()
+    box = (samp // per).to(torch.int32)
+    pot = torch.zeros(len(samp), dtype=torch.float64, device=dev)
+    ctx.evaluate(0, len(samp), pts, f.leaf_locals(), f.S, nleaf, f.leaf_centres, pot, box=box)
+    allp = pos.reshape(-1, 3)
+    allq = q.reshape(-1)
+    direct = torch.zeros(len(samp), dtype=torch.float64, device=dev)
+    for c0 in range(0, len(allp), 1 << 18):
+        r = torch.cdist(pts, allp[c0:c0 + (1 << 18)], compute_mode="donot_use_mm_for_euclid_dist")
+        direct += torch.where(r > 0, allq[c0:c0 + (1 << 18)][None, :] / r.clamp_min(1e-300),
+                              torch.zeros_like(r)).sum(1)
+    ns, nt = fmm.neighbours(depth, dev)
+    near = torch.zeros(len(samp), dtype=torch.float64, device=dev)
+    for i in range(len(samp)):
+        b = int(box[i])
+        srcb = ns[nt == b]
+        idx = (srcb[:, None] * per + torch.arange(per, device=dev)[None, :]).reshape(-1)
+        r = torch.linalg.norm(allp[idx] - pts[i], dim=1)
+        near[i] = torch.where(r > 0, allq[idx] / r.clamp_min(1e-300), torch.zeros_like(r)).sum()
+    phys = float(torch.linalg.norm(pot + near - direct) / torch.linalg.norm(direct))
+    # leaf locals against the oracle's CPU pass
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fmm_oracle
+    import pyoracle
+
+    pyoracle.build(with_ref=False)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import norm_weights, rel_err
+
+    qh, ph = q.cpu().numpy(), pos.cpu().numpy()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = fmm_oracle.fmm_pass(depth, P, qh, ph, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    w = norm_weights(P, "L")
+    err_split = rel_err(f.leaf_locals().cpu().numpy(), ref, w)
+    fp.run(q, pos)
+    torch.cuda.synchronize()
+    err_plain = rel_err(fp.leaf_locals().cpu().numpy(), ref, w)
+    line = {"metric": FMM_METRIC, "value": ms, "unit": "ms per pass", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "split (int32 block fixed point rotations, float-float z-translation, "
+                                          "f64 accumulation)",
+            "data": "synthetic (seeded uniform charges in every leaf)",
+            "config": {"workload": "uniform octree depth 5 on [0,1]^3, 32 768 leaves x 32 charges U[-1,1], P=12",
+                       "translations_per_pass": counts, "l2": "expansions of all levels (93 MB) fit in L2",
+                       "parallelism": f"replicas x{world}"},
+            "translations_per_s": ntr / (ms * 1e-3), "plain_fp64_ms_per_pass": ms_plain,
+            "leaf_local_rel_err_vs_oracle_pass": {"split": err_split, "plain_fp64": err_plain,
+                                                   "metric": "max over leaves, relative L2, orthonormal basis"},
+            "potential_rel_err_vs_direct_2000_particles": phys,
+            "cpu_baseline": {"value": cpu_s * 1e3, "unit": "ms per pass", "cores": threads, "kind": "port",
+                             "sample": "the same pass (P2M + all translations) by the oracle's FP64 rotation-method "
+                                       "port, one pthread per core"},
+            "clocks": clk, "gpu_launches": launches}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -388,6 +507,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "mixed":
         return run_mixed(args)
+    if args.workload == "fmm":
+        return run_fmm(args)
     op, P, N, nq = WORKLOADS[args.workload]
     world, rank, local = dist_init(args)
     config = {"workload": f"{op.upper()} P={P} (reference order: degrees 0..{P - 1}), {N} translations per GPU, "
