@@ -670,7 +670,9 @@ def main():
                          "note": "float-float throughout (relative error ~1e-13)"},
             "accuracy_vs_fp64_oracle_1000": acc,
             "e2e": {"value": world * N / e2e_s, "unit": "translations/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "api": "sfmm_translate_host_packed (pinned host buffers)"},
+                    "d2h_bytes_per_step": d2h,
+                    "api": "sfmm_translate_host_packed on pinned host buffers: the kernel reads the sources and "
+                           "updates the targets in place over the host link (bytes counted are those crossing it)"},
             "roofline": roof, "roofline_compute": roof_compute, "roofline_plain_fp64": roof_fp64,
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
     print(json.dumps(line))

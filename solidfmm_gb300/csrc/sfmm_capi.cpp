@@ -159,6 +159,18 @@ int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound)
     return SFMM_OK;
 }
 
+const void *device_view(sfmm_context *c, const void *host)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeHost && at.devicePointer && at.device == c->device) return at.devicePointer;
+    if (at.type == cudaMemoryTypeUnregistered && c->pageable_access) return host;
+    return nullptr;
+}
+
 // The launch itself: validated arguments, device pointers.
 int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound, long long n, const void *src,
               long long sstride, long long nsrc, const uint32_t *sidx, void *dst, long long dstride, long long ndst,
@@ -340,6 +352,11 @@ int sfmm_create(sfmm_context **out, int dtype, size_t P, int device)
     c->device = device;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) == cudaSuccess)
+            c->pageable_access = v != 0;
+    }
     if (e != cudaSuccess) {
         delete c;
         return SFMM_CUDA_ERROR;
@@ -652,6 +669,35 @@ int sfmm_translate_host_packed(sfmm_context *c, int op, int precision, size_t n,
         if (!c->pipe[k] && (e = cudaStreamCreateWithFlags(&c->pipe[k], cudaStreamNonBlocking)) != cudaSuccess)
             return cuda_fail(c, e, "stream create");
     const bool pipelined = !src_index && !dst_index;
+    // Zero-copy: when the caller's arrays are device-accessible (pinned host
+    // memory, or any host memory where the GPU walks the host page tables, as
+    // over GB300's NVLink-C2C), the kernel reads the sources and updates the
+    // targets in place over the host link.  The link carries the same bytes
+    // as the staged copies, but the kernel's reads and writes overlap on it
+    // fully (45 vs 37 M translations/s at P=16).  Batches with repeated
+    // targets keep their atomics in device memory (staged path).
+    if (pipelined && !(flags & SFMM_TARGETS_REPEAT)) {
+        const void *vs = device_view(c, src);
+        void *vd = const_cast<void *>(device_view(c, dst));
+        if (vs && vd) {
+            if ((e = c->d_meta[0].ensure(n * 2 * sizeof(uint32_t))) != cudaSuccess ||
+                (e = c->d_shift[0].ensure(n * 3 * sizeof(double))) != cudaSuccess)
+                return cuda_fail(c, e, "device buffers");
+            uint32_t *dm = (uint32_t *)c->d_meta[0].p;
+            double *dsh = (double *)c->d_shift[0].p;
+            cudaStream_t s = c->pipe[0];
+            if ((e = cudaMemcpyAsync(dm, p_in, n * 4, cudaMemcpyHostToDevice, s)) ||
+                (e = cudaMemcpyAsync(dm + n, p_out, n * 4, cudaMemcpyHostToDevice, s)) ||
+                (e = cudaMemcpyAsync(dsh, shift, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s)))
+                return cuda_fail(c, e, "host-to-device copy");
+            st = run_batch(c, s, op, a, (int)pmax, (long long)n, vs, (long long)src_stride, (long long)src_count,
+                           nullptr, vd, (long long)dst_stride, (long long)dst_count, nullptr, dm, dm + n, dsh, nullptr,
+                           flags);
+            if (st) return st;
+            if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "synchronise");
+            return SFMM_OK;
+        }
+    }
     // chunk of translations per pipeline step
     size_t chunk = pipelined ? std::max<size_t>(8192, (n + 23) / 24) : n;
     if (chunk > n) chunk = n;

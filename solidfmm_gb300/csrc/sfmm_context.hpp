@@ -87,6 +87,7 @@ struct sfmm_context {
     cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
     std::map<std::pair<int, int>, sfmm::LaunchShape> shapes;  // (arith, order bound) -> launch shape
     int *d_woff = nullptr, *d_hoff = nullptr;            // table offsets (shared by all arithmetics)
+    bool pageable_access = false;  // the GPU reads pageable host memory through the host page tables
 };
 
 namespace sfmm {
@@ -98,6 +99,10 @@ int cuda_fail(sfmm_context *c, cudaError_t e, const char *what);
 int arith_of(sfmm_context *c, int precision, Arith *out);
 // upload the arithmetic's tables once
 int ensure_tables(sfmm_context *c, Arith a);
+// device address of a caller's host array when the kernels can use it
+// directly (pinned host memory, or pageable memory on a GPU that uses the host
+// page tables), else nullptr
+const void *device_view(sfmm_context *c, const void *host);
 // tables and launch shape of (arithmetic, order bound) for op, so that a
 // launch makes no allocation (plans call this before a graph capture)
 int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound);

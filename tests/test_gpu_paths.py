@@ -109,6 +109,35 @@ def test_host_packed_matches_device(native, ctx64):
     assert np.array_equal(dev, host)
 
 
+@pytest.mark.parametrize("memory", ["pinned", "pageable"])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_host_packed_zero_copy_and_staged(native, ctx64, oracle, memory, prec):
+    """Host-packed batches run in place on device-accessible host memory
+    (pinned, or pageable where the GPU uses the host page tables) and through
+    staged copies otherwise (repeated targets); both match the oracle."""
+    import torch
+
+    b = _batch("m2l", (2, 16), (2, 16), 3000, 61)
+    ref = _oracle(oracle, "m2l", b)
+    w = norm_weights(16, "L")
+    tol = 1e-11 if prec == 0 else 1e-7
+    if memory == "pinned":
+        src = torch.as_tensor(b["src"]).pin_memory()
+        host = torch.as_tensor(b["dst"].copy()).pin_memory()
+    else:
+        src, host = b["src"].copy(), b["dst"].copy()
+    ctx64.translate_host_packed("m2l", prec, src, host, b["Pin"], b["Pout"], b["xyz"])
+    got = host.numpy() if memory == "pinned" else host
+    assert rel_err(got - b["dst"], ref - b["dst"], w) < tol
+    # repeated targets through index arrays: staged copies, atomics on the device
+    r = _batch("m2l", (2, 16), (2, 16), 600, 62, pattern="repeat")
+    rref = _oracle(oracle, "m2l", r)
+    host = r["dst"].copy()
+    ctx64.translate_host_packed("m2l", prec, r["src"], host, r["Pin"], r["Pout"], r["xyz"], src_index=r["sidx"],
+                                dst_index=r["tidx"], repeat=True)
+    assert rel_err(host - r["dst"], rref - r["dst"], w) < tol
+
+
 @pytest.mark.parametrize("kind", [0, 1])
 def test_p2x_device_vs_oracle(native, oracle, kind):
     import torch
