@@ -47,6 +47,9 @@ WORKLOADS = {
     # one FMM pass: uniform octree of depth 5 (32 768 leaves) on the unit cube,
     # 32 charges U[-1, 1] per leaf, P=12
     "fmm": ("fmm", 12, 32768, 32),
+    # M2M, M2L, L2L at P=20, FP64 (plain, split, split_ff) and FP32, 1e6 each;
+    # plus M2L at P=16 and P=17 (the other reading of "order")
+    "ops20": ("ops20", 20, 1_000_000, 128),
 }
 
 METRIC = "M2L translations/s at P=16, chosen vs plain FP64 GPU at equal rel. error; %roofline"
@@ -379,6 +382,82 @@ def run_mixed(args):
     print(json.dumps(line))
 
 
+OPS_METRIC = "translations/s per operator and arithmetic, P=20, 1e6 translations"
+
+
+def run_ops20(args):
+    """Every operator at P=20 in every arithmetic (1e6 translations, 128
+    charges per source), with the relative error against the FP64 naive
+    oracle on 500 translations; M2L at P=16 and P=17 beside it.  FP32 at
+    P=20 is above the reference's float limit (18) and is checked against the
+    FP64 oracle."""
+    import torch
+    import solidfmm_gb300 as sf
+    from solidfmm_gb300 import build as _b
+
+    world, rank, local = dist_init(args)
+    _b.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle
+    from helpers import norm_weights, rel_err
+
+    pyoracle.build(with_ref=False)
+    rows = []
+    for op, P, N in (("m2m", 20, 1_000_000), ("m2l", 20, 1_000_000), ("l2l", 20, 1_000_000),
+                     ("m2l", 16, 1_000_000), ("m2l", 17, 1_000_000)):
+        S = P * (P + 1)
+        ctx = sf.Context(P, "f64", device=local)
+        ctx32 = sf.Context(P, "f32", device=local)
+        stream = torch.cuda.current_stream(dev)
+        ctx.set_stream(stream.cuda_stream)
+        ctx32.set_stream(stream.cuda_stream)
+        src, shift, pin = make_inputs(ctx, op, P, N, 128 if P == 20 else 64, 321 + rank, dev)
+        src32 = src.to(torch.float32)
+        dst = torch.zeros(N, S, dtype=torch.float64, device=dev)
+        dst32 = torch.zeros(N, S, dtype=torch.float32, device=dev)
+        nsub = 500
+        ref = np.zeros((nsub, S))
+        pinh = pin[:nsub].cpu().numpy().astype(np.uint32)
+        pyoracle.naive(op, src[:nsub].cpu().numpy(), pinh, ref, pinh, shift[:nsub].cpu().numpy())
+        w = norm_weights(P, "M" if op == "m2m" else "L")
+        for name, c, prec, sb, db in (("plain_fp64", ctx, 0, src, dst), ("split", ctx, 1, src, dst),
+                                      ("split_ff", ctx, 2, src, dst), ("plain_fp32", ctx32, 0, src32, dst32)):
+            def f():
+                c.translate_device(op, prec, N, sb, S, N, db, S, N, pin, pin, shift)
+            for _ in range(args.warmup):
+                f()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(max(2, args.steps // 4)):
+                f()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = allmax(world, e0.elapsed_time(e1) / max(2, args.steps // 4), dev)
+            d = torch.zeros(nsub, S, dtype=db.dtype, device=dev)
+            c.translate_device(op, prec, nsub, sb[:nsub].contiguous(), S, nsub, d, S, nsub, pin[:nsub].contiguous(),
+                               pin[:nsub].contiguous(), shift[:nsub].contiguous())
+            got = d.double().cpu().numpy()
+            rows.append({"op": op, "P": P, "arith": name, "translations_per_s": world * N / (ms * 1e-3),
+                         "rel_err_orthonormal_max": rel_err(got, ref, w), "rel_err_raw_max": rel_err(got, ref)})
+        del src, src32, dst, dst32, ctx, ctx32
+        torch.cuda.empty_cache()
+    if rank != 0:
+        return
+    head = next(r for r in rows if r["op"] == "m2l" and r["P"] == 20 and r["arith"] == "split")
+    line = {"metric": OPS_METRIC, "value": head["translations_per_s"], "unit": "translations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "per row", "data": "synthetic (seeded P2M/P2L of random charges)",
+            "config": {"workload": "M2M/M2L/L2L at P=20 (1e6 each, 128 charges per source), M2L at P=16 and 17",
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+            "rows": rows}
+    print(json.dumps(line))
+
+
 FMM_METRIC = "FMM pass time (P2M + M2M + M2L + L2L), uniform octree depth 5, P=12, 32 charges per leaf"
 
 
@@ -509,6 +588,8 @@ def main():
         return run_mixed(args)
     if args.workload == "fmm":
         return run_fmm(args)
+    if args.workload == "ops20":
+        return run_ops20(args)
     op, P, N, nq = WORKLOADS[args.workload]
     world, rank, local = dist_init(args)
     config = {"workload": f"{op.upper()} P={P} (reference order: degrees 0..{P - 1}), {N} translations per GPU, "

@@ -239,12 +239,14 @@ LaunchShape translate_shape(Arith a, int P, int G, int ts)
     s.G = G;
     s.acc = acc;
     int scap = P * (P + 1) + 4;  // room for the swap loops' zero-coefficient reads past the last row
-    // Translation stride in shared memory: the translations of a warp read
-    // the same element offset at once (all threads of a group, two adjacent
-    // slots); strides of 2 (mod 16) 8-byte slots or 4 (mod 32) 4-byte slots
-    // start consecutive translations 4 banks apart, so those reads are
-    // conflict-free.
-    const int mod = esize(a) == 8 ? 16 : 32, want = esize(a) == 8 ? 2 : 4;
+    // Translation stride in shared memory.  The swap and z loops read one or
+    // two slots per translation, broadcast to its group; the per-element
+    // stages touch G consecutive slots per translation.  With 8 translations
+    // per warp (G = 4) bases 4 banks apart keep the broadcasts conflict-free;
+    // with 4 per warp (G = 8) bases 8 banks apart keep both patterns at the
+    // minimum number of wavefronts.
+    const int mod = esize(a) == 8 ? 16 : 32;
+    const int want = esize(a) == 8 ? (G == 8 ? 4 : 2) : (G == 8 ? 8 : 4);
     s.spad = scap + ((want - scap) % mod + mod) % mod;
     s.TS = ts;
     s.threads = G * ts;
