@@ -58,6 +58,11 @@ METRIC = "M2L translations/s at P=16, chosen vs plain FP64 GPU at equal rel. err
 # (dram__bytes_read.sum + dram__bytes_write.sum over the launch / 65 536
 # translations, workload m2l16_small); see profiles/
 TRAFFIC = {("m2l", 16): 5716.0}
+# warp instructions per translation of the split kernel from the same capture
+# (smsp__inst_executed.sum / 65 536): the kernel is issue bound, so its
+# instruction rate against one warp instruction per cycle per SM sub-partition
+# is the roofline that bounds it
+INSTRUCTIONS = {("m2l", 16): 8373.0}
 
 
 def useful_flops(op, P):
@@ -716,6 +721,16 @@ def main():
                                f"{tb:.0f} B per translation on 65 536 translations, scaled to {N}") if tb else None,
             "peak_source": peak_src, "kernel": "k_translate<ff, G, ACC, fixed> (split)",
             "bytes_per_translation": B}
+    roof_issue = None
+    ipt = INSTRUCTIONS.get((op, P))
+    if ipt and clk and clk.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_issue = sms * 4 * clk["sm_mhz"] * 1e6
+        roof_issue = {"bound": "instruction issue", "unit": "warp instructions/s",
+                      "instructions_per_translation": ipt, "achieved": ipt / t_kernel, "peak": peak_issue,
+                      "frac": ipt / t_kernel / peak_issue,
+                      "peak_source": f"{sms} SMs x 4 schedulers x 1 instruction/cycle at the sampled {clk['sm_mhz']} MHz",
+                      "instructions_source": "ncu smsp__inst_executed.sum of the split kernel / 65 536 translations"}
     # the split path does FP64-class work on the FP32 and integer pipes: its
     # useful flop rate set against the FP64 pipe's measured peak (a ratio
     # above 1 is beyond any FP64 kernel's reach)
@@ -754,7 +769,8 @@ def main():
                     "d2h_bytes_per_step": d2h,
                     "api": "sfmm_translate_host_packed on pinned host buffers: the kernel reads the sources and "
                            "updates the targets in place over the host link (bytes counted are those crossing it)"},
-            "roofline": roof, "roofline_compute": roof_compute, "roofline_plain_fp64": roof_fp64,
+            "roofline": roof, "roofline_issue": roof_issue, "roofline_compute": roof_compute,
+            "roofline_plain_fp64": roof_fp64,
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
     print(json.dumps(line))
 
