@@ -153,7 +153,7 @@ struct Trig {
 
 // One degree of the forward transform, NA = ceil(d / G) blocks.
 template <class AR, int G, int NA, int ACC>
-__device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, int rowpad,
+__device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n,
                                                const typename AR::T *__restrict__ WR,
                                                const typename AR::T *__restrict__ ein, typename AR::T f, int q,
                                                const Trig<AR, ACC> &tg)
@@ -209,7 +209,7 @@ __device__ __forceinline__ void forward_degree(typename AR::Stor *b, int n, int 
 
 // One degree of the backward transform, NA = ceil(d / G) blocks.
 template <class AR, int G, int NA, int ACC>
-__device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n, int rowpad,
+__device__ __forceinline__ void backward_degree(typename AR::Stor *b, int n,
                                                 const typename AR::T *__restrict__ WR,
                                                 const typename AR::T *__restrict__ eout, typename AR::T f, int q,
                                                 const Trig<AR, ACC> &tg)
@@ -270,7 +270,7 @@ __device__ __forceinline__ void st_fixed(float2 *p, int v) { *reinterpret_cast<i
 // exponent, integer swap, renormalise, integer rotation, integer swap,
 // renormalise, back to float-float.
 template <int G, int NA, int ACC>
-__device__ __forceinline__ void forward_degree_fixed(float2 *b, int n, int rowpad, const int *__restrict__ WRq,
+__device__ __forceinline__ void forward_degree_fixed(float2 *b, int n, const int *__restrict__ WRq,
                                                      const ff *__restrict__ ein, ff f, int q,
                                                      const Trig<arith<ff>, ACC> &tg, const FixTrig<ACC> &tq)
 {
@@ -334,7 +334,7 @@ __device__ __forceinline__ void forward_degree_fixed(float2 *b, int n, int rowpa
 // One degree of the backward transform with fixed-point swaps and beta
 // rotation; the alpha rotation and r-power scale stay in float-float.
 template <int G, int NA, int ACC>
-__device__ __forceinline__ void backward_degree_fixed(float2 *b, int n, int rowpad, const int *__restrict__ WRq,
+__device__ __forceinline__ void backward_degree_fixed(float2 *b, int n, const int *__restrict__ WRq,
                                                       const ff *__restrict__ eout, ff f, int q,
                                                       const Trig<arith<ff>, ACC> &tg, const FixTrig<ACC> &tq)
 {
@@ -675,12 +675,12 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             if constexpr (FIX) {
                 const int *WRq = p.Wq + __ldg(p.woff + n);
                 dispatch<ACC>((n + G) / G, [&](auto na) {
-                    forward_degree_fixed<G, decltype(na)::value, ACC>(b, n, p.rowpad, WRq, ein, f, q, tg, tq);
+                    forward_degree_fixed<G, decltype(na)::value, ACC>(b, n, WRq, ein, f, q, tg, tq);
                 });
             } else {
                 const T *WR = W + __ldg(p.woff + n);
                 dispatch<ACC>((n + G) / G, [&](auto na) {
-                    forward_degree<AR, G, decltype(na)::value, ACC>(b, n, p.rowpad, WR, ein, f, q, tg);
+                    forward_degree<AR, G, decltype(na)::value, ACC>(b, n, WR, ein, f, q, tg);
                 });
             }
             if (kFF) f = AR::mul(f, rstep);
@@ -716,12 +716,12 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             if constexpr (FIX) {
                 const int *WRq = p.Wq + __ldg(p.woff + n);
                 dispatch<ACC>((n + G) / G, [&](auto na) {
-                    backward_degree_fixed<G, decltype(na)::value, ACC>(b, n, p.rowpad, WRq, eo, f, q, tg, tq);
+                    backward_degree_fixed<G, decltype(na)::value, ACC>(b, n, WRq, eo, f, q, tg, tq);
                 });
             } else {
                 const T *WR = W + __ldg(p.woff + n);
                 dispatch<ACC>((n + G) / G, [&](auto na) {
-                    backward_degree<AR, G, decltype(na)::value, ACC>(b, n, p.rowpad, WR, eo, f, q, tg);
+                    backward_degree<AR, G, decltype(na)::value, ACC>(b, n, WR, eo, f, q, tg);
                 });
             }
             if (kFF) fo = AR::mul(fo, qstep);

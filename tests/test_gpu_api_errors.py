@@ -1,0 +1,87 @@
+"""Argument checking of the C ABI's newer entry points on a GPU context:
+evaluation, tuning and plans report errors through their status codes and
+leave their outputs untouched; empty plans run and launch nothing."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx8(native):
+    return native.Context(8, "f64")
+
+
+def test_eval_errors(native, ctx8):
+    import torch
+
+    dev = torch.device("cuda", 0)
+    S = 72
+    pts = torch.zeros(4, 3, dtype=torch.float64, device=dev)
+    E = torch.zeros(4, S, dtype=torch.float64, device=dev)
+    cen = torch.zeros(4, 3, dtype=torch.float64, device=dev)
+    pot = torch.zeros(4, dtype=torch.float64, device=dev)
+    grad = torch.zeros(4, 3, dtype=torch.float64, device=dev)
+    with pytest.raises(native.SfmmError, match="UNSUPPORTED"):
+        ctx8.evaluate(1, 4, pts, E, S, 4, cen, pot, gradient=grad)
+    with pytest.raises(native.SfmmError, match="INVALID_ARG"):
+        ctx8.evaluate(0, 4, pts, E, S - 1, 4, cen, pot)
+    with pytest.raises(native.SfmmError, match="INVALID_ARG"):
+        ctx8.evaluate(0, 4, pts, E, S, 3, cen, pot)          # fewer expansions than points, no box index
+    with pytest.raises(native.SfmmError, match="INVALID_ARG"):
+        ctx8.evaluate(2, 4, pts, E, S, 4, cen, pot)
+    ctx8.evaluate(0, 0, pts, E, S, 4, cen, pot)                # nothing to do
+    torch.cuda.synchronize()
+    assert float(pot.abs().sum()) == 0.0
+
+
+def test_tune_and_group_errors(native, ctx8):
+    with pytest.raises(native.SfmmError, match="INVALID_ARG"):
+        ctx8.tune("m2l", 0, n=0)
+    with pytest.raises(native.SfmmError, match="ORDER_RANGE"):
+        ctx8.tune("m2l", 0, n=1024, order_bound=9)
+    with pytest.raises(native.SfmmError, match="INVALID_ARG"):
+        ctx8.tune(7, 0, n=1024)
+    with pytest.raises(native.SfmmError, match="ORDER_RANGE"):
+        ctx8.set_group(0, 4, order_bound=9)
+    f32 = native.Context(8, "f32")
+    with pytest.raises(native.SfmmError, match="UNSUPPORTED"):
+        f32.tune("m2l", 1, n=1024)
+    g, rate = ctx8.tune("l2l", 0, n=4096)
+    assert g in (4, 8) and rate > 0
+
+
+def test_empty_plan_and_empty_stage(native, ctx8):
+    import torch
+
+    dev = torch.device("cuda", 0)
+    plan = native.Plan(ctx8).finalize()
+    plan.run()
+    assert plan.launches == 0 and plan.segments() == []
+    S = 72
+    src = torch.ones(2, S, dtype=torch.float64, device=dev)
+    dst = torch.zeros(2, S, dtype=torch.float64, device=dev)
+    o = torch.full((2,), 8, dtype=torch.int32, device=dev)
+    sh = torch.ones(2, 3, dtype=torch.float64, device=dev)
+    plan = native.Plan(ctx8)
+    plan.add("m2l", 0, 0, src, S, 2, dst, S, 2, o, o, sh)        # empty stage
+    plan.add("m2l", 0, 2, src, S, 2, dst, S, 2, o, o, sh)
+    plan.finalize()
+    plan.run()
+    torch.cuda.synchronize()
+    assert plan.launches == 1
+    assert float(dst.abs().sum()) > 0
+
+
+def test_host_packed_zero_orders(native, ctx8):
+    """Zero orders on the in-place host path: nothing is added to the target."""
+    rng = np.random.default_rng(2)
+    n, S = 64, 72
+    src = rng.normal(size=(n, S))
+    dst = rng.normal(size=(n, S))
+    before = dst.copy()
+    pin = np.zeros(n, np.uint32)
+    pout = np.full(n, 8, np.uint32)
+    xyz = rng.normal(size=(n, 3)) + 3
+    ctx8.translate_host_packed("m2l", 0, src, dst, pin, pout, xyz)
+    assert np.array_equal(dst, before)
