@@ -175,7 +175,8 @@ const void *device_view(sfmm_context *c, const void *host)
 int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound, long long n, const void *src,
               long long sstride, long long nsrc, const uint32_t *sidx, void *dst, long long dstride, long long ndst,
               const uint32_t *tidx, const uint32_t *pin, const uint32_t *pout, const double *shift,
-              const uint32_t *perm, int flags, long long nidx)
+              const uint32_t *perm, int flags, long long nidx, const unsigned long long *src_ptr,
+              const unsigned long long *dst_ptr)
 {
     if (n == 0) return SFMM_OK;
     a = resolve_arith(a, op, Pbound);
@@ -203,6 +204,8 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.shift = shift;
     p.perm = perm;
     p.nidx = nidx < 0 ? n : nidx;
+    p.src_ptr = src_ptr;
+    p.dst_ptr = dst_ptr;
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
     p.W = t.W;
     p.Wq = static_cast<const int *>(t.Wq);
@@ -322,6 +325,37 @@ int translate_blocks_per_sm(Arith a, const LaunchShape &s)
 }
 
 }  // namespace sfmm
+
+namespace {
+
+// Open-addressing map from target addresses to dense slots: the classic host
+// call may name one target solid many times.
+struct AddrSlots {
+    std::vector<unsigned long long> key;
+    std::vector<uint32_t> val;
+    size_t mask = 0;
+    explicit AddrSlots(size_t n)
+    {
+        size_t cap = 64;
+        while (cap < 2 * n) cap <<= 1;
+        key.assign(cap, 0);
+        val.assign(cap, 0);
+        mask = cap - 1;
+    }
+    // the slot of address k (non-zero), adding `next` if k is new; second =
+    // whether it was added
+    std::pair<uint32_t, bool> find_or_add(unsigned long long k, uint32_t next)
+    {
+        size_t h = (size_t)(((k >> 3) * 0x9E3779B97F4A7C15ull) >> 20) & mask;
+        while (key[h] && key[h] != k) h = (h + 1) & mask;
+        if (key[h]) return {val[h], false};
+        key[h] = k;
+        val[h] = next;
+        return {next, true};
+    }
+};
+
+}  // namespace
 
 extern "C" {
 
@@ -766,96 +800,150 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
     }
     const size_t es = c->dtype == SFMM_F64 ? 8 : 4;
     const size_t stride = pmax * (pmax + 1);
-    const size_t N = n * dim;
-    // unique targets: (solid pointer, component) -> slot; sources are copied per translation
-    std::unordered_map<const void *, uint32_t> tslot;
-    std::vector<const char *> tptr;
-    std::vector<size_t> tord;
-    std::vector<uint32_t> tidx(N), pin(N), pout(N);
-    std::vector<double> sh(3 * N);
+    // One entry per (translation, component) that has work (a zero order adds
+    // nothing); targets named more than once share a slot.
+    std::vector<unsigned long long> sptr, dptr, tptr;
+    std::vector<uint32_t> pin, pout, tidx, tcnt;
+    std::vector<double> sh;
     bool repeat = false;
     try {
-        tslot.reserve(N);
-        for (size_t i = 0; i < n; ++i)
+        const size_t N = n * dim;
+        sptr.reserve(N);
+        dptr.reserve(N);
+        pin.reserve(N);
+        pout.reserve(N);
+        tidx.reserve(N);
+        sh.reserve(3 * N);
+        AddrSlots slots(N);
+        for (size_t i = 0; i < n; ++i) {
+            if (!p_in[i] || !p_out[i]) continue;
+            const size_t ci = p_in[i] * (p_in[i] + 1), co = p_out[i] * (p_out[i] + 1);
+            double xyz[3];
+            const void *arr[3] = {x, y, z};
+            for (int j = 0; j < 3; ++j)
+                xyz[j] = c->dtype == SFMM_F64 ? ((const double *)arr[j])[i] : (double)((const float *)arr[j])[i];
             for (size_t d = 0; d < dim; ++d) {
-                size_t k = i * dim + d;
-                const char *tp = (const char *)dst[i] + d * p_out[i] * (p_out[i] + 1) * es;
-                auto it = tslot.find(tp);
-                if (it == tslot.end()) {
-                    it = tslot.emplace(tp, (uint32_t)tptr.size()).first;
+                const unsigned long long sp = (unsigned long long)(uintptr_t)src[i] + d * ci * es;
+                const unsigned long long tp = (unsigned long long)(uintptr_t)dst[i] + d * co * es;
+                const auto r = slots.find_or_add(tp, (uint32_t)tptr.size());
+                if (r.second) {
                     tptr.push_back(tp);
-                    tord.push_back(p_out[i]);
+                    tcnt.push_back((uint32_t)co);
                 } else {
                     repeat = true;
                 }
-                tidx[k] = it->second;
-                pin[k] = (uint32_t)p_in[i];
-                pout[k] = (uint32_t)p_out[i];
-                for (int j = 0; j < 3; ++j) {
-                    const void *arr = j == 0 ? x : (j == 1 ? y : z);
-                    sh[3 * k + j] = c->dtype == SFMM_F64 ? ((const double *)arr)[i] : (double)((const float *)arr)[i];
-                }
+                sptr.push_back(sp);
+                dptr.push_back(tp);
+                tidx.push_back(r.first);
+                pin.push_back((uint32_t)p_in[i]);
+                pout.push_back((uint32_t)p_out[i]);
+                sh.insert(sh.end(), xyz, xyz + 3);
             }
+        }
     } catch (const std::bad_alloc &) {
         return fail(c, SFMM_OOM, "host bookkeeping");
     }
-    const size_t nt = tptr.size();
+    const size_t M = sptr.size(), nt = tptr.size();
+    if (M == 0) return SFMM_OK;
     std::lock_guard<std::mutex> lock(c->mtx);
     cudaSetDevice(c->device);
     cudaError_t e;
-    if ((e = c->h_src.ensure(N * stride * es)) || (e = c->h_dst.ensure(nt * stride * es)))
-        return cuda_fail(c, e, "pinned staging");
-    if ((e = c->d_src[0].ensure(N * stride * es)) || (e = c->d_dst[0].ensure(nt * stride * es)) ||
-        (e = c->d_meta[0].ensure(N * 3 * sizeof(uint32_t))) || (e = c->d_shift[0].ensure(N * 3 * sizeof(double))))
-        return cuda_fail(c, e, "device buffers");
-    // gather sources (solid2buf of the whole batch) with a few host threads
-    char *hs = (char *)c->h_src.p;
-    auto gather = [&](size_t lo, size_t hi) {
-        for (size_t k = lo; k < hi; ++k) {
-            size_t i = k / dim, d = k % dim;
-            size_t cnt = p_in[i] * (p_in[i] + 1);
-            if (cnt) std::memcpy(hs + k * stride * es, (const char *)src[i] + d * cnt * es, cnt * es);
-        }
-    };
-    size_t nthr = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), N / 4096 + 1);
-    nthr = std::min<size_t>(nthr, 16);
-    if (nthr <= 1) {
-        gather(0, N);
-    } else {
-        std::vector<std::thread> th;
-        for (size_t t = 0; t < nthr; ++t) th.emplace_back(gather, N * t / nthr, N * (t + 1) / nthr);
-        for (auto &t : th) t.join();
-    }
-    uint32_t *dm = (uint32_t *)c->d_meta[0].p;
     cudaStream_t s = c->stream;
-    if ((e = cudaMemcpyAsync(c->d_src[0].p, hs, N * stride * es, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemsetAsync(c->d_dst[0].p, 0, nt * stride * es, s)) ||
-        (e = cudaMemcpyAsync(dm, tidx.data(), N * 4, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemcpyAsync(dm + N, pin.data(), N * 4, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemcpyAsync(dm + 2 * N, pout.data(), N * 4, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemcpyAsync(c->d_shift[0].p, sh.data(), N * 3 * sizeof(double), cudaMemcpyHostToDevice, s)))
+    const size_t toff = (M * 28 + 7) & ~(size_t)7;  // 8-byte aligned start of the slot addresses
+    if ((e = c->d_meta[0].ensure(toff + nt * 12)) || (e = c->d_shift[0].ensure(M * 3 * sizeof(double))))
+        return cuda_fail(c, e, "device buffers");
+    // metadata: source addresses | target addresses | p_in | p_out | target slots | slot addresses | slot sizes
+    char *mb = (char *)c->d_meta[0].p;
+    auto *d_sptr = (unsigned long long *)mb;
+    auto *d_dptr = d_sptr + M;
+    auto *d_pin = (uint32_t *)(d_dptr + M);
+    uint32_t *d_pout = d_pin + M, *d_tidx = d_pin + 2 * M;
+    auto *d_tptr = (unsigned long long *)(mb + toff);
+    uint32_t *d_tcnt = (uint32_t *)(d_tptr + nt);
+    const double *d_sh = (const double *)c->d_shift[0].p;
+    if ((e = cudaMemcpyAsync(d_sptr, sptr.data(), M * 8, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(d_dptr, dptr.data(), M * 8, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(d_pin, pin.data(), M * 4, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(d_pout, pout.data(), M * 4, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(d_tidx, tidx.data(), M * 4, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync((void *)d_sh, sh.data(), M * 3 * sizeof(double), cudaMemcpyHostToDevice, s)))
         return cuda_fail(c, e, "host-to-device copy");
-    st = run_batch(c, s, op, a, (int)pmax, (long long)N, c->d_src[0].p, (long long)stride, (long long)N, nullptr,
-                   c->d_dst[0].p, (long long)stride, (long long)nt, dm, dm + N, dm + 2 * N,
-                   (const double *)c->d_shift[0].p, nullptr, repeat ? SFMM_TARGETS_REPEAT : SFMM_TARGETS_UNIQUE);
-    if (st) return st;
+    if (c->pageable_access) {
+        // The GPU reads the source solids and updates the target solids where
+        // they are, through the host page tables: no staging copies.
+        if (!repeat) {
+            st = run_batch(c, s, op, a, (int)pmax, (long long)M, nullptr, 0, (long long)M, nullptr, nullptr, 0,
+                           (long long)M, nullptr, d_pin, d_pout, d_sh, nullptr, SFMM_TARGETS_UNIQUE, -1, d_sptr,
+                           d_dptr);
+            if (st) return st;
+        } else {
+            // repeated targets: sums per target in device slots (atomics),
+            // then one read-modify-write of each host target
+            if ((e = cudaMemcpyAsync(d_tptr, tptr.data(), nt * 8, cudaMemcpyHostToDevice, s)) ||
+                (e = cudaMemcpyAsync(d_tcnt, tcnt.data(), nt * 4, cudaMemcpyHostToDevice, s)))
+                return cuda_fail(c, e, "host-to-device copy");
+            if ((e = c->d_dst[0].ensure(nt * stride * es)) || (e = cudaMemsetAsync(c->d_dst[0].p, 0, nt * stride * es, s)))
+                return cuda_fail(c, e, "device buffers");
+            st = run_batch(c, s, op, a, (int)pmax, (long long)M, nullptr, 0, (long long)M, nullptr, c->d_dst[0].p,
+                           (long long)stride, (long long)nt, d_tidx, d_pin, d_pout, d_sh, nullptr, SFMM_TARGETS_REPEAT,
+                           -1, d_sptr, nullptr);
+            if (st) return st;
+            if ((e = launch_add_slots(c->dtype == SFMM_F64, (long long)nt, d_tptr, d_tcnt, c->d_dst[0].p,
+                                      (long long)stride, s)) != cudaSuccess)
+                return cuda_fail(c, e, "target accumulation kernel");
+            c->launches++;
+        }
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "synchronise");
+        return SFMM_OK;
+    }
+    // Staged path (the GPU cannot use pageable host memory): gather the
+    // sources into pinned staging, translate into per-target slots, copy the
+    // slots back and add them into the host targets.
+    if ((e = c->h_src.ensure(M * stride * es)) || (e = c->h_dst.ensure(nt * stride * es)))
+        return cuda_fail(c, e, "pinned staging");
+    if ((e = c->d_src[0].ensure(M * stride * es)) || (e = c->d_dst[0].ensure(nt * stride * es)))
+        return cuda_fail(c, e, "device buffers");
+    char *hs = (char *)c->h_src.p;
     char *hd = (char *)c->h_dst.p;
+    const size_t nthr = std::min<size_t>(std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 16),
+                                         M / 4096 + 1);
+    auto parallel = [&](size_t cnt, auto &&fn) {
+        if (nthr <= 1) {
+            fn(0, cnt);
+            return;
+        }
+        std::vector<std::thread> th;
+        for (size_t t = 0; t < nthr; ++t) th.emplace_back(fn, cnt * t / nthr, cnt * (t + 1) / nthr);
+        for (auto &t : th) t.join();
+    };
+    parallel(M, [&](size_t lo, size_t hi) {
+        for (size_t k = lo; k < hi; ++k)
+            std::memcpy(hs + k * stride * es, (const void *)(uintptr_t)sptr[k], (size_t)pin[k] * (pin[k] + 1) * es);
+    });
+    if ((e = cudaMemcpyAsync(c->d_src[0].p, hs, M * stride * es, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemsetAsync(c->d_dst[0].p, 0, nt * stride * es, s)))
+        return cuda_fail(c, e, "host-to-device copy");
+    st = run_batch(c, s, op, a, (int)pmax, (long long)M, c->d_src[0].p, (long long)stride, (long long)M, nullptr,
+                   c->d_dst[0].p, (long long)stride, (long long)nt, d_tidx, d_pin, d_pout, d_sh, nullptr,
+                   repeat ? SFMM_TARGETS_REPEAT : SFMM_TARGETS_UNIQUE);
+    if (st) return st;
     if ((e = cudaMemcpyAsync(hd, c->d_dst[0].p, nt * stride * es, cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
         return cuda_fail(c, e, "device-to-host copy");
-    // scatter-add into the host targets (buf2solid)
-    for (size_t j = 0; j < nt; ++j) {
-        size_t cnt = tord[j] * (tord[j] + 1);
-        if (c->dtype == SFMM_F64) {
-            double *o = (double *)tptr[j];
-            const double *r = (const double *)(hd + j * stride * es);
-            for (size_t q = 0; q < cnt; ++q) o[q] += r[q];
-        } else {
-            float *o = (float *)tptr[j];
-            const float *r = (const float *)(hd + j * stride * es);
-            for (size_t q = 0; q < cnt; ++q) o[q] += r[q];
+    // scatter-add into the host targets (buf2solid); targets are distinct
+    parallel(nt, [&](size_t lo, size_t hi) {
+        for (size_t j = lo; j < hi; ++j) {
+            if (c->dtype == SFMM_F64) {
+                double *o = (double *)(uintptr_t)tptr[j];
+                const double *r = (const double *)(hd + j * stride * es);
+                for (size_t q = 0; q < tcnt[j]; ++q) o[q] += r[q];
+            } else {
+                float *o = (float *)(uintptr_t)tptr[j];
+                const float *r = (const float *)(hd + j * stride * es);
+                for (size_t q = 0; q < tcnt[j]; ++q) o[q] += r[q];
+            }
         }
-    }
+    });
     return SFMM_OK;
 }
 

@@ -48,6 +48,10 @@ cudaError_t launch_eval(bool f64, int kind, int P, long long npts, const double 
                         const void *E, long long stride, const double *centre, double *pot, double *grad,
                         cudaStream_t st);
 
+// target[j] += slots[j] for unique host targets given by address (sfmm_p2x.cu)
+cudaError_t launch_add_slots(bool f64, long long nt, const unsigned long long *tptr, const uint32_t *cnt,
+                             const void *slots, long long stride, cudaStream_t st);
+
 // bucketing by order pair (sfmm_p2x.cu)
 cudaError_t launch_bucket(long long n, const uint32_t *pin, const uint32_t *pout, uint32_t *order,
                           uint32_t *work, int P, cudaStream_t st);

@@ -243,6 +243,36 @@ cudaError_t launch_eval(bool f64, int kind, int P, long long npts, const double 
     return cudaGetLastError();
 }
 
+// ---- accumulation of per-target results into targets given by address ----
+//
+// One warp per target: target[c] += slots[j * stride + c] for c < cnt[j].
+// The targets are distinct, so plain read-modify-writes suffice; they may be
+// host solids that the GPU reads and writes through the host page tables.
+template <class T>
+__global__ void k_add_slots(long long nt, const unsigned long long *__restrict__ tptr,
+                            const uint32_t *__restrict__ cnt, const T *__restrict__ slots, long long stride)
+{
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nt) return;
+    T *o = reinterpret_cast<T *>(tptr[w]);
+    const T *r = slots + w * stride;
+    for (uint32_t c = lane; c < cnt[w]; c += 32) o[c] += r[c];
+}
+
+cudaError_t launch_add_slots(bool f64, long long nt, const unsigned long long *tptr, const uint32_t *cnt,
+                             const void *slots, long long stride, cudaStream_t st)
+{
+    if (nt == 0) return cudaSuccess;
+    const int tb = 256;
+    const long long grid = (nt * 32 + tb - 1) / tb;
+    if (f64)
+        k_add_slots<double><<<(unsigned)grid, tb, 0, st>>>(nt, tptr, cnt, (const double *)slots, stride);
+    else
+        k_add_slots<float><<<(unsigned)grid, tb, 0, st>>>(nt, tptr, cnt, (const float *)slots, stride);
+    return cudaGetLastError();
+}
+
 // ---- bucketing by (p_in, p_out) ----
 
 __global__ void k_bucket_count(long long n, const uint32_t *pin, const uint32_t *pout, uint32_t *cnt, int K)

@@ -38,6 +38,12 @@ struct KParams {
     int TS;             // translations per CTA tile
     void *scratch;      // global buffer (GBUF kernels)
     int *status;        // device error word: bit 0 = a translation had an out-of-range index or order
+    // pointer mode (both null otherwise): translation t reads its source at
+    // src_ptr[t] and accumulates into dst_ptr[t] (addresses the GPU can use,
+    // e.g. host solids on a GPU that walks the host page tables); sidx/tidx
+    // are then null and nsrc = ndst = nidx
+    const unsigned long long *src_ptr;
+    const unsigned long long *dst_ptr;
 };
 
 }  // namespace sfmm

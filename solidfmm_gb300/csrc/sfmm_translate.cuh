@@ -644,7 +644,8 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         for (int s = warp; s < TS; s += nwarps) {
             const int ps = (int)m_pin[s];
             const int cnt = ps * (ps + 1);
-            const Src *sp = src + (long long)m_sidx[s] * p.sstride;
+            const Src *sp = p.src_ptr ? reinterpret_cast<const Src *>(p.src_ptr[m_sidx[s]])
+                                      : src + (long long)m_sidx[s] * p.sstride;
             S *bp = buf0 + (long long)s * p.spad;
             for (int c = lane; c < p.spad; c += 32) AR::st(bp + c, c < cnt ? AR::from_src(__ldcs(sp + c)) : AR::zero());
         }
@@ -736,8 +737,9 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             const int cnt = max(po * (po + 1), pid * (pid + 1));
             if (!cnt) continue;
             const S *bp = buf0 + (long long)s * p.spad;
-            const Src *sp = src + (long long)m_sidx[s] * p.sstride;
-            Src *dp = dst + (long long)m_tidx[s] * p.dstride;
+            const Src *sp = p.src_ptr ? reinterpret_cast<const Src *>(p.src_ptr[m_sidx[s]])
+                                      : src + (long long)m_sidx[s] * p.sstride;
+            Src *dp = p.dst_ptr ? reinterpret_cast<Src *>(p.dst_ptr[m_tidx[s]]) : dst + (long long)m_tidx[s] * p.dstride;
             for (int c = lane; c < cnt; c += 32) {
                 if constexpr (AR::split) {
                     // hi and lo widen by exponent re-biasing; two FP64 additions

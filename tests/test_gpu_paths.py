@@ -260,3 +260,55 @@ def test_dropin_cxx_program(native, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     print(r.stdout)
     assert r.returncode == 0, r.stdout[-4000:] + r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("pattern", ["distinct", "repeat"])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_classic_host_call_pointer_batches(native, oracle, pattern, prec):
+    """sfmm_translate_host (the classic call over arrays of solid pointers,
+    dim = 2 components): distinct and repeated targets, mixed orders with
+    zeros, against the oracle per component."""
+    import ctypes as C
+
+    L = native.load()
+    rng = np.random.default_rng(71 if pattern == "distinct" else 72)
+    b = _batch("m2l", (0, 12), (0, 12), 240, 73, pattern=pattern)
+    n = len(b["Pin"])
+    dim = 2
+    ctx = native.Context(12, "f64")
+    # every solid is its own allocation with dim components of P(P+1) reals
+    srcs = [np.concatenate([b["src"][b["sidx"][i], :int(b["Pin"][i]) * (int(b["Pin"][i]) + 1)],
+                            -2.0 * b["src"][b["sidx"][i], :int(b["Pin"][i]) * (int(b["Pin"][i]) + 1)]])
+            for i in range(n)]
+    nt = int(b["tidx"].max()) + 1
+    tord = np.zeros(nt, np.int64)
+    tord[b["tidx"]] = b["Pout"]
+    tgts = [rng.normal(size=dim * int(tord[j]) * (int(tord[j]) + 1)) for j in range(nt)]
+    before = [t.copy() for t in tgts]
+    sp = (C.c_void_p * n)(*[s.ctypes.data if s.size else None for s in srcs])
+    dp = (C.c_void_p * n)(*[tgts[int(b["tidx"][i])].ctypes.data if tgts[int(b["tidx"][i])].size else None
+                            for i in range(n)])
+    pin = (C.c_size_t * n)(*[int(v) for v in b["Pin"]])
+    pout = (C.c_size_t * n)(*[int(tord[int(b["tidx"][i])]) for i in range(n)])
+    x, y, z = (np.ascontiguousarray(b["xyz"][:, k]) for k in range(3))
+    L.sfmm_translate_host.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p]
+    rc = L.sfmm_translate_host(ctx.h, 1, prec, n, sp, pin, dp, pout, dim, x.ctypes.data, y.ctypes.data,
+                               z.ctypes.data)
+    assert rc == 0, L.sfmm_last_error(ctx.h)
+    S = 156
+    for comp, scale in ((0, 1.0), (1, -2.0)):
+        src = scale * b["src"]
+        ref = np.zeros((nt, S))
+        for j in range(nt):
+            c = int(tord[j]) * (int(tord[j]) + 1)
+            ref[j, :c] = before[j][comp * c:(comp + 1) * c]
+        start = ref.copy()
+        oracle.naive("m2l", src, b["Pin"], ref, np.array([tord[int(t)] for t in b["tidx"]], np.uint32), b["xyz"],
+                     sidx=b["sidx"], tidx=b["tidx"])
+        got = np.zeros((nt, S))
+        for j in range(nt):
+            c = int(tord[j]) * (int(tord[j]) + 1)
+            got[j, :c] = tgts[j][comp * c:(comp + 1) * c]
+        tol = 1e-11 if prec == 0 else 1e-7
+        assert rel_err(got - start, ref - start, norm_weights(12, "L")) < tol, comp
