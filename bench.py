@@ -699,6 +699,30 @@ def main():
     h2d = N * S * 8 * 2 + N * 8 + N * 24
     d2h = N * S * 8
 
+    # the classic call (sfmm_translate_host, what the drop-in
+    # multithreaded_translator and m2l(op, buf, howmany, M**, L**, ...) use):
+    # arrays of solid addresses, here the rows of the same pinned buffers
+    Lb = sf.load()
+    Lb.sfmm_translate_host.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p]
+    addr_s = np.uint64(h_src.data_ptr()) + np.arange(N, dtype=np.uint64) * np.uint64(S * 8)
+    addr_d = np.uint64(h_dst.data_ptr()) + np.arange(N, dtype=np.uint64) * np.uint64(S * 8)
+    ord64 = h_pin.astype(np.uint64)
+    sx, sy, sz = (np.ascontiguousarray(h_shift[:, k]) for k in range(3))
+    opc = {"m2m": 0, "m2l": 1, "l2l": 2}[op]
+
+    def classic():
+        rc = Lb.sfmm_translate_host(ctx.h, opc, 1, N, addr_s.ctypes.data, ord64.ctypes.data, addr_d.ctypes.data,
+                                    ord64.ctypes.data, 1, sx.ctypes.data, sy.ctypes.data, sz.ctypes.data)
+        assert rc == 0, Lb.sfmm_last_error(ctx.h)
+
+    classic()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        classic()
+    classic_s = allmax(world, (time.perf_counter() - t0) / e2e_steps, dev)
+
     acc = accuracy(ctx, op, P, src, shift, pin, 1000, dev) if rank == 0 else None
 
     if rank != 0:
@@ -769,6 +793,10 @@ def main():
                     "d2h_bytes_per_step": d2h,
                     "api": "sfmm_translate_host_packed on pinned host buffers: the kernel reads the sources and "
                            "updates the targets in place over the host link (bytes counted are those crossing it)"},
+            "e2e_classic_call": {"value": world * N / classic_s, "unit": "translations/s",
+                                 "api": "sfmm_translate_host: arrays of N source and target solid addresses (the "
+                                        "drop-in classic and multithreaded_translator calls), in place over the "
+                                        "host link"},
             "roofline": roof, "roofline_issue": roof_issue, "roofline_compute": roof_compute,
             "roofline_plain_fp64": roof_fp64,
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
