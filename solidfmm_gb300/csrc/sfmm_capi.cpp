@@ -143,20 +143,30 @@ Arith resolve_arith(Arith a, int op, int Pbound)
     return a;
 }
 
-int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound)
+int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound, LaunchShape *shape)
 {
     a = resolve_arith(a, op, Pbound);
     if (Pbound < 1) Pbound = 1;
+    std::lock_guard<std::mutex> lk(c->setup_mtx);
     int st = ensure_tables(c, a);
     if (st) return st;
     const auto key = std::make_pair((int)a, Pbound);
     auto it = c->shapes.find(key);
     if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound, default_group(a, Pbound))).first;
+    if (shape) *shape = it->second;
     if (it->second.acc == 0)
         return fail(c, SFMM_UNSUPPORTED, "order %d exceeds the GPU kernels' limit %d", Pbound, kMaxKernelOrder);
     if (a != Arith::F64 && Pbound > kMaxFloatOrder)
         return fail(c, SFMM_UNSUPPORTED, "order %d exceeds %d, the limit of FP32-range arithmetic", Pbound, kMaxFloatOrder);
     return SFMM_OK;
+}
+
+// replace (or, with nullptr, drop) a cached launch shape
+void set_shape(sfmm_context *c, std::pair<int, int> key, const LaunchShape *s)
+{
+    std::lock_guard<std::mutex> lk(c->setup_mtx);
+    if (s) c->shapes[key] = *s;
+    else c->shapes.erase(key);
 }
 
 const void *device_view(sfmm_context *c, const void *host)
@@ -181,9 +191,9 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     if (n == 0) return SFMM_OK;
     a = resolve_arith(a, op, Pbound);
     if (Pbound < 1) Pbound = 1;
-    int st = prepare_launch(c, op, a, Pbound);
+    LaunchShape s;
+    int st = prepare_launch(c, op, a, Pbound, &s);
     if (st) return st;
-    const LaunchShape s = c->shapes.find(std::make_pair((int)a, Pbound))->second;
     const DevTables &t = c->tab[(int)a];
     KParams p{};
     p.op = op;
@@ -437,7 +447,7 @@ void sfmm_destroy(sfmm_context *c)
 size_t sfmm_order(const sfmm_context *c) { return c ? (size_t)c->P : 0; }
 int sfmm_data_type(const sfmm_context *c) { return c ? c->dtype : -1; }
 const char *sfmm_last_error(const sfmm_context *c) { return c ? c->err.c_str() : "null context"; }
-uint64_t sfmm_launch_count(const sfmm_context *c) { return c ? c->launches : 0; }
+uint64_t sfmm_launch_count(const sfmm_context *c) { return c ? c->launches.load() : 0; }
 
 int sfmm_host_table(size_t P, int which, int n, double *out, size_t cap, size_t *count)
 {
@@ -490,6 +500,7 @@ int sfmm_set_group(sfmm_context *c, int precision, size_t order_bound, int group
     if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, SFMM_CUDA_ERROR, "cannot select device %d", c->device);
     LaunchShape s = best_shape(a, Pb, group);
     if (!s.acc) return fail(c, SFMM_INVALID_ARG, "no kernel runs %d threads per translation at order %d", group, Pb);
+    std::lock_guard<std::mutex> lk2(c->setup_mtx);
     c->shapes[std::make_pair((int)a, Pb)] = s;
     return SFMM_OK;
 }
@@ -551,7 +562,7 @@ int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t
     for (int G : groups) {
         LaunchShape s = best_shape(a, Pb, G);
         if (!s.acc) continue;
-        c->shapes[key] = s;
+        set_shape(c, key, &s);
         float ms = 0;
         for (int rep = 0; rep < 2 && st == SFMM_OK; ++rep) {  // warm-up, then timed
             if (rep == 1 && (e = cudaEventRecord(e0, stream)) != cudaSuccess) break;
@@ -563,7 +574,7 @@ int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t
         if (st == SFMM_OK && e == cudaSuccess && (e = cudaEventSynchronize(e1)) == cudaSuccess)
             e = cudaEventElapsedTime(&ms, e0, e1);
         if (st != SFMM_OK || e != cudaSuccess) {
-            c->shapes.erase(key);
+            set_shape(c, key, nullptr);
             cleanup();
             return st != SFMM_OK ? st : cuda_fail(c, e, "tuning run");
         }
@@ -575,10 +586,10 @@ int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t
     }
     cleanup();
     if (!best.acc) {
-        c->shapes.erase(key);
+        set_shape(c, key, nullptr);
         return fail(c, SFMM_UNSUPPORTED, "no kernel for order %d", Pb);
     }
-    c->shapes[key] = best;
+    set_shape(c, key, &best);
     if (group) *group = best.G;
     if (rate) *rate = best_rate;
     return SFMM_OK;

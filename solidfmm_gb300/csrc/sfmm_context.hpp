@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <map>
 #include <mutex>
@@ -78,8 +79,9 @@ struct sfmm_context {
     sfmm::HostTables host;
     sfmm::DevTables tab[4];  // indexed by Arith
     std::string err;
-    uint64_t launches = 0;
+    std::atomic<uint64_t> launches{0};
     std::mutex mtx;  // serialises host-path calls (one translator object, one stream)
+    std::mutex setup_mtx;  // table uploads and the launch-shape cache (device calls may come from several threads)
     int *d_status = nullptr;  // device error word of the translation kernels
     // host-path staging (three pipeline slots for the packed host call)
     sfmm::DevBuf d_src[3], d_dst[3], d_meta[3], d_shift[3], d_work;
@@ -105,7 +107,7 @@ int ensure_tables(sfmm_context *c, Arith a);
 const void *device_view(sfmm_context *c, const void *host);
 // tables and launch shape of (arithmetic, order bound) for op, so that a
 // launch makes no allocation (plans call this before a graph capture)
-int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound);
+int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound, LaunchShape *shape = nullptr);
 // one validated translation launch on device pointers (translation i of the
 // batch is perm[i] when perm is given)
 int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound, long long n, const void *src,

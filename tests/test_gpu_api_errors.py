@@ -85,3 +85,48 @@ def test_host_packed_zero_orders(native, ctx8):
     xyz = rng.normal(size=(n, 3)) + 3
     ctx8.translate_host_packed("m2l", 0, src, dst, pin, pout, xyz)
     assert np.array_equal(dst, before)
+
+
+def test_concurrent_device_calls_share_a_context(native):
+    """Device calls from several host threads on one context, each at an
+    order bound not used before (first use uploads tables and builds the
+    launch shape): every thread's result equals a sequential run."""
+    import threading
+
+    import torch
+
+    dev = torch.device("cuda", 0)
+    P = 20
+    ctx = native.Context(P, "f64")
+    S = P * (P + 1)
+    rng = np.random.default_rng(9)
+    jobs = []
+    for k, (bound, prec) in enumerate([(6, 0), (9, 1), (12, 2), (15, 1), (18, 0), (20, 2)]):
+        n = 500
+        src = torch.as_tensor(rng.normal(size=(n, S)) * 1e-2, device=dev)
+        o = torch.full((n,), bound, dtype=torch.int32, device=dev)
+        u = rng.normal(size=(n, 3))
+        sh = torch.as_tensor(u / np.linalg.norm(u, axis=1, keepdims=True) * 3.0, device=dev)
+        jobs.append((bound, prec, n, src, o, sh))
+    out = [None] * len(jobs)
+
+    def work(i):
+        bound, prec, n, src, o, sh = jobs[i]
+        st = torch.cuda.Stream(dev)
+        with torch.cuda.stream(st):
+            d = torch.zeros(n, S, dtype=torch.float64, device=dev)
+            st.synchronize()
+            ctx.translate_device("m2l", prec, n, src, S, n, d, S, n, o, o, sh, order_bound=bound)
+            torch.cuda.synchronize()
+            out[i] = d.cpu().numpy()
+
+    th = [threading.Thread(target=work, args=(i,)) for i in range(len(jobs))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for i, (bound, prec, n, src, o, sh) in enumerate(jobs):
+        d = torch.zeros(n, S, dtype=torch.float64, device=dev)
+        ctx.translate_device("m2l", prec, n, src, S, n, d, S, n, o, o, sh, order_bound=bound)
+        torch.cuda.synchronize()
+        assert np.array_equal(out[i], d.cpu().numpy()), bound
