@@ -54,6 +54,11 @@ struct cd {
 };
 __device__ __forceinline__ cd cmul(cd a, cd b) { return cd{a.c * b.c - a.s * b.s, a.s * b.c + a.c * b.s}; }
 
+__device__ __forceinline__ void prefetch_l2(const void *ptr)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+}
+
 template <int N>
 struct ic {
     static constexpr int value = N;
@@ -650,6 +655,31 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             for (int c = lane; c < p.spad; c += 32) AR::st(bp + c, c < cnt ? AR::from_src(__ldcs(sp + c)) : AR::zero());
         }
         __syncthreads();
+
+        // L2 prefetch, spread over the group: this tile's targets (read at the
+        // end of the tile) and the next tile's sources (read at its start),
+        // so that both phases meet L2 instead of DRAM.  Device arrays only;
+        // every address lies inside an expansion the entry may touch.
+        if (!p.src_ptr) {
+            const int tc = max(pout * (pout + 1), ident_p * (ident_p + 1));
+            if (valid && tc) {
+                const char *dp = reinterpret_cast<const char *>(dst + (long long)ti * p.dstride);
+                for (int o = q * 128; o < tc * (int)sizeof(Src); o += G * 128) prefetch_l2(dp + o);
+            }
+            const long long i2 = (tile + gridDim.x) * TS + slot;
+            if (i2 < p.n) {
+                const uint32_t t2 = p.perm ? p.perm[i2] : (uint32_t)i2;
+                if (t2 < p.nidx) {
+                    const uint32_t s2 = p.sidx ? p.sidx[t2] : t2;
+                    const int pin2 = (int)p.pin[t2];
+                    if (s2 < p.nsrc && pin2 > 0 && pin2 <= P) {
+                        const char *sp2 = reinterpret_cast<const char *>(src + (long long)s2 * p.sstride);
+                        for (int o = q * 128; o < pin2 * (pin2 + 1) * (int)sizeof(Src); o += G * 128)
+                            prefetch_l2(sp2 + o);
+                    }
+                }
+            }
+        }
 
         S *b = buf0 + (long long)slot * p.spad;
         const int pin_w = __reduce_max_sync(FULL, pin);
