@@ -142,8 +142,10 @@ int sfmm_translate_host(sfmm_context *ctx, int op, int precision, size_t n,
  * or 8 for order bounds up to 32, one warp (32) above.  By default a context
  * takes G per (precision, order bound) from a built-in table measured on
  * GB300; sfmm_set_group pins G for one (precision, order bound) pair, and
- * sfmm_tune times every supported G on n synthetic translations of `op` on
- * the context's stream (synchronising it) and keeps the fastest.  `group`
+ * sfmm_tune times every supported G, each with the largest and the smallest
+ * tile (translations per CTA) that keep the SM fully occupied, on n synthetic
+ * translations of `op` on the context's stream (synchronising it) and keeps
+ * the fastest.  `group`
  * (may be NULL) receives the kept G, `rate` (may be NULL) its measured
  * translations per second.  order_bound 0 = the context order. */
 int sfmm_set_group(sfmm_context *ctx, int precision, size_t order_bound, int group);

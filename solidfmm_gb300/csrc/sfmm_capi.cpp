@@ -287,8 +287,9 @@ int default_group(Arith a, int P)
 
 // The tile size that keeps the most threads resident per SM (shared memory
 // and registers permitting) for G threads per translation; ties go to the
-// larger tile.
-LaunchShape best_shape(Arith a, int P, int G)
+// larger tile (fewer CTAs), or to the smaller one with small_tiles (shorter
+// waits at the tile barriers).
+LaunchShape best_shape(Arith a, int P, int G, bool small_tiles)
 {
     LaunchShape best;
     long best_threads = 0;
@@ -297,7 +298,7 @@ LaunchShape best_shape(Arith a, int P, int G)
         if (!s.acc) continue;
         s.blocks_per_sm = translate_blocks_per_sm(a, s);
         long th = (long)s.blocks_per_sm * s.threads;
-        if (th > best_threads) {
+        if (th > best_threads || (small_tiles && th == best_threads)) {
             best_threads = th;
             best = s;
         }
@@ -559,9 +560,11 @@ int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t
     LaunchShape best;
     double best_rate = 0;
     const int groups[] = {4, 8, 32};
-    for (int G : groups) {
-        LaunchShape s = best_shape(a, Pb, G);
+    for (int cand = 0; cand < 6; ++cand) {
+        const int G = groups[cand / 2];
+        LaunchShape s = best_shape(a, Pb, G, cand & 1);
         if (!s.acc) continue;
+        if ((cand & 1) && s.TS == best_shape(a, Pb, G, false).TS) continue;  // the same shape twice
         set_shape(c, key, &s);
         float ms = 0;
         for (int rep = 0; rep < 2 && st == SFMM_OK; ++rep) {  // warm-up, then timed

@@ -33,7 +33,7 @@ struct LaunchShape {
 
 LaunchShape translate_shape(Arith a, int P, int G, int ts);
 int default_group(Arith a, int P);
-LaunchShape best_shape(Arith a, int P, int G);
+LaunchShape best_shape(Arith a, int P, int G, bool small_tiles = false);
 
 // Launch the fused translation kernel (defined in sfmm_k{64,32,ff,ffq}.cu).
 cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, int grid, cudaStream_t st);
