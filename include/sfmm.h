@@ -138,6 +138,14 @@ int sfmm_translate_host(sfmm_context *ctx, int op, int precision, size_t n,
                         void *const *dst, const size_t *p_out, size_t dim,
                         const void *x, const void *y, const void *z);
 
+/* Minimal bounding sphere on the host (the reference's bounding_sphere,
+ * solidfmm/sphere.hpp:38-42): the smallest sphere containing n points
+ * (r NULL) or n spheres of radii r[i]; out = {x, y, z, radius}.  n == 0 ->
+ * SFMM_INVALID_ARG; a degenerate configuration that floating point cannot
+ * resolve -> SFMM_UNSUPPORTED (the reference throws std::runtime_error). */
+int sfmm_bounding_sphere(size_t n, const double *x, const double *y, const double *z, const double *r,
+                         double *out);
+
 /* Launch shape.  The translation kernels run G threads per translation: 4
  * or 8 for order bounds up to 32, one warp (32) above.  By default a context
  * takes G per (precision, order bound) from a built-in table measured on

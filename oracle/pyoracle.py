@@ -85,6 +85,7 @@ def ref(native=False):
         L.ref_swap_B.restype = C.c_double
         L.ref_dot_d.argtypes = [C.c_size_t, C.c_size_t, _f64p, C.c_size_t, C.c_size_t, _f64p, _f64p]
         L.ref_hw_threads.restype = C.c_uint
+        L.ref_bounding_sphere_d.argtypes = [C.c_size_t, _f64p, _f64p, _f64p, C.c_void_p, _f64p]
         _ref[path] = L
     return _ref[path]
 

@@ -23,6 +23,7 @@
 #include <solidfmm/harmonics.hpp>
 #include <solidfmm/translations.hpp>
 #include <solidfmm/swap_matrix.hpp>
+#include <solidfmm/sphere.hpp>
 
 #include <chrono>
 #include <cstdint>
@@ -203,5 +204,33 @@ double ref_swap_B(int n, int m, int l)
 unsigned ref_hw_threads()
 {
     return std::thread::hardware_concurrency();
+}
+
+// the reference's bounding_sphere over points (r == NULL) or spheres; 0 = ok,
+// 1 = std::logic_error, 2 = other exception
+int ref_bounding_sphere_d(size_t n, const double *x, const double *y, const double *z, const double *r,
+                          double *out)
+{
+    try {
+        sphere<double> s;
+        if (!r) {
+            s = bounding_sphere(n, x, y, z);
+        } else {
+            std::vector<sphere<double>> v(n);
+            for (size_t i = 0; i < n; ++i) v[i] = sphere<double>{x[i], y[i], z[i], r[i]};
+            s = bounding_sphere(v.data(), v.data() + n);
+        }
+        out[0] = s.x;
+        out[1] = s.y;
+        out[2] = s.z;
+        out[3] = s.r;
+        return 0;
+    } catch (const std::logic_error &e) {
+        std::snprintf(g_err, sizeof g_err, "%s", e.what());
+        return 1;
+    } catch (const std::exception &e) {
+        std::snprintf(g_err, sizeof g_err, "%s", e.what());
+        return 2;
+    }
 }
 }

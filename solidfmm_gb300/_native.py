@@ -28,7 +28,7 @@ EXPORTS = [
     "sfmm_translate_host", "sfmm_bucket_by_order", "sfmm_p2x_device", "sfmm_launch_count",
     "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak", "sfmm_bucket_by_order_noalloc",
     "sfmm_set_group", "sfmm_tune", "sfmm_plan_create", "sfmm_plan_add", "sfmm_plan_finalize", "sfmm_plan_run",
-    "sfmm_plan_launches", "sfmm_plan_segments", "sfmm_plan_destroy", "sfmm_eval_device",
+    "sfmm_plan_launches", "sfmm_plan_segments", "sfmm_plan_destroy", "sfmm_eval_device", "sfmm_bounding_sphere",
 ]
 
 
@@ -83,6 +83,7 @@ def load():
     L.sfmm_measure_imad_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.sfmm_bucket_by_order_noalloc.argtypes = [sz, u32p, u32p, u32p, sz, vp]
     L.sfmm_eval_device.argtypes = [vp, C.c_int, sz, dp, u32p, vp, sz, sz, dp, dp, dp]
+    L.sfmm_bounding_sphere.argtypes = [sz, dp, dp, dp, dp, dp]
     L.sfmm_plan_create.argtypes = [vp, C.POINTER(vp)]
     L.sfmm_plan_add.argtypes = [vp, C.c_int, C.c_int, sz, vp, sz, sz, u32p, vp, sz, sz, u32p, u32p, u32p, dp,
                                 C.c_int]
@@ -107,6 +108,20 @@ def host_table(P: int, which: int, n: int = 0) -> np.ndarray:
         raise SfmmError(rc, "sfmm_host_table")
     out = np.zeros(cnt.value)
     L.sfmm_host_table(P, which, n, out.ctypes.data, cnt.value, C.byref(cnt))
+    return out
+
+
+def bounding_sphere(x, y, z, r=None):
+    """Smallest sphere containing the points (x, y, z), or the spheres of
+    radii r: (cx, cy, cz, radius) (sfmm_bounding_sphere; host only)."""
+    L = load()
+    x, y, z = (np.ascontiguousarray(a, np.float64) for a in (x, y, z))
+    rr = None if r is None else np.ascontiguousarray(r, np.float64)
+    out = np.zeros(4)
+    rc = L.sfmm_bounding_sphere(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data,
+                                None if rr is None else rr.ctypes.data, out.ctypes.data)
+    if rc:
+        raise SfmmError(rc, "bounding_sphere")
     return out
 
 
