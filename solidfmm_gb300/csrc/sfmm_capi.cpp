@@ -337,37 +337,6 @@ int translate_blocks_per_sm(Arith a, const LaunchShape &s)
 
 }  // namespace sfmm
 
-namespace {
-
-// Open-addressing map from target addresses to dense slots: the classic host
-// call may name one target solid many times.
-struct AddrSlots {
-    std::vector<unsigned long long> key;
-    std::vector<uint32_t> val;
-    size_t mask = 0;
-    explicit AddrSlots(size_t n)
-    {
-        size_t cap = 64;
-        while (cap < 2 * n) cap <<= 1;
-        key.assign(cap, 0);
-        val.assign(cap, 0);
-        mask = cap - 1;
-    }
-    // the slot of address k (non-zero), adding `next` if k is new; second =
-    // whether it was added
-    std::pair<uint32_t, bool> find_or_add(unsigned long long k, uint32_t next)
-    {
-        size_t h = (size_t)(((k >> 3) * 0x9E3779B97F4A7C15ull) >> 20) & mask;
-        while (key[h] && key[h] != k) h = (h + 1) & mask;
-        if (key[h]) return {val[h], false};
-        key[h] = k;
-        val[h] = next;
-        return {next, true};
-    }
-};
-
-}  // namespace
-
 extern "C" {
 
 const char *sfmm_status_string(int s)
@@ -805,82 +774,79 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
     if (st) return st;
     if (n == 0 || dim == 0) return SFMM_OK;
     if (!src || !dst || !p_in || !p_out || !x || !y || !z) return fail(c, SFMM_INVALID_ARG, "null host pointer");
-    size_t pmax = 1;
-    for (size_t i = 0; i < n; ++i) {
-        if (p_in[i] > (size_t)c->P || p_out[i] > (size_t)c->P)
-            return fail(c, SFMM_ORDER_RANGE, "orders exceeding operator data (translation %zu)", i);
-        if ((p_in[i] && !src[i]) || (p_out[i] && !dst[i])) return fail(c, SFMM_INVALID_ARG, "null solid pointer");
-        pmax = std::max(pmax, std::max(p_in[i], p_out[i]));
+    ClassicInput in;
+    in.n = n;
+    in.src = src;
+    in.p_in = p_in;
+    in.dst = dst;
+    in.p_out = p_out;
+    in.dim = dim;
+    in.x = x;
+    in.y = y;
+    in.z = z;
+    in.f64 = c->dtype == SFMM_F64;
+    in.P = (size_t)c->P;
+    ClassicScan sc;
+    try {
+        sc = classic_scan(in, host_threads(n * dim));
+    } catch (const std::exception &) {
+        return fail(c, SFMM_OOM, "host threads");
     }
-    const size_t es = c->dtype == SFMM_F64 ? 8 : 4;
-    const size_t stride = pmax * (pmax + 1);
+    if (sc.bad != SIZE_MAX) {
+        if (sc.bad_kind == 1)
+            return fail(c, SFMM_ORDER_RANGE, "orders exceeding operator data (translation %zu)", sc.bad);
+        return fail(c, SFMM_INVALID_ARG, "null solid pointer");
+    }
     // One entry per (translation, component) that has work (a zero order adds
     // nothing); targets named more than once share a slot.
-    std::vector<unsigned long long> sptr, dptr, tptr;
-    std::vector<uint32_t> pin, pout, tidx, tcnt;
-    std::vector<double> sh;
-    bool repeat = false;
-    try {
-        const size_t N = n * dim;
-        sptr.reserve(N);
-        dptr.reserve(N);
-        pin.reserve(N);
-        pout.reserve(N);
-        tidx.reserve(N);
-        sh.reserve(3 * N);
-        AddrSlots slots(N);
-        for (size_t i = 0; i < n; ++i) {
-            if (!p_in[i] || !p_out[i]) continue;
-            const size_t ci = p_in[i] * (p_in[i] + 1), co = p_out[i] * (p_out[i] + 1);
-            double xyz[3];
-            const void *arr[3] = {x, y, z};
-            for (int j = 0; j < 3; ++j)
-                xyz[j] = c->dtype == SFMM_F64 ? ((const double *)arr[j])[i] : (double)((const float *)arr[j])[i];
-            for (size_t d = 0; d < dim; ++d) {
-                const unsigned long long sp = (unsigned long long)(uintptr_t)src[i] + d * ci * es;
-                const unsigned long long tp = (unsigned long long)(uintptr_t)dst[i] + d * co * es;
-                const auto r = slots.find_or_add(tp, (uint32_t)tptr.size());
-                if (r.second) {
-                    tptr.push_back(tp);
-                    tcnt.push_back((uint32_t)co);
-                } else {
-                    repeat = true;
-                }
-                sptr.push_back(sp);
-                dptr.push_back(tp);
-                tidx.push_back(r.first);
-                pin.push_back((uint32_t)p_in[i]);
-                pout.push_back((uint32_t)p_out[i]);
-                sh.insert(sh.end(), xyz, xyz + 3);
-            }
-        }
-    } catch (const std::bad_alloc &) {
-        return fail(c, SFMM_OOM, "host bookkeeping");
-    }
-    const size_t M = sptr.size(), nt = tptr.size();
+    const size_t M = sc.entries;
     if (M == 0) return SFMM_OK;
+    if (M >= ((size_t)1 << 31)) return fail(c, SFMM_INVALID_ARG, "more than 2^31 translations in one call");
+    const size_t pmax = sc.pmax;
+    const size_t es = c->dtype == SFMM_F64 ? 8 : 4;
+    const size_t stride = pmax * (pmax + 1);
     std::lock_guard<std::mutex> lock(c->mtx);
     cudaSetDevice(c->device);
     cudaError_t e;
     cudaStream_t s = c->stream;
-    const size_t toff = (M * 28 + 7) & ~(size_t)7;  // 8-byte aligned start of the slot addresses
-    if ((e = c->d_meta[0].ensure(toff + nt * 12)) || (e = c->d_shift[0].ensure(M * 3 * sizeof(double))))
+    // metadata, in pinned staging and on the device alike: source addresses |
+    // target addresses | p_in | p_out | target slots | (8-byte aligned) slot
+    // addresses [M] | slot sizes [M]; shifts separately
+    const size_t toff = (M * 28 + 7) & ~(size_t)7;
+    const size_t meta_bytes = toff + M * 12;
+    if ((e = c->h_meta.ensure(meta_bytes)) || (e = c->h_shift.ensure(M * 3 * sizeof(double))))
+        return cuda_fail(c, e, "pinned staging");
+    if ((e = c->d_meta[0].ensure(meta_bytes)) || (e = c->d_shift[0].ensure(M * 3 * sizeof(double))))
         return cuda_fail(c, e, "device buffers");
-    // metadata: source addresses | target addresses | p_in | p_out | target slots | slot addresses | slot sizes
+    char *hm = (char *)c->h_meta.p;
+    ClassicEntries ent;
+    ent.sptr = (unsigned long long *)hm;
+    ent.dptr = ent.sptr + M;
+    ent.pin = (uint32_t *)(ent.dptr + M);
+    ent.pout = ent.pin + M;
+    ent.tidx = ent.pin + 2 * M;
+    ent.tptr = (unsigned long long *)(hm + toff);
+    ent.tcnt = (uint32_t *)(ent.tptr + M);
+    ent.shift = (double *)c->h_shift.p;
+    bool repeat = false;
+    size_t nt = 0;
+    try {
+        nt = classic_fill(in, sc, ent, c->slot_scratch, &repeat);
+    } catch (const std::bad_alloc &) {
+        return fail(c, SFMM_OOM, "host bookkeeping");
+    } catch (const std::exception &) {
+        return fail(c, SFMM_OOM, "host threads");
+    }
     char *mb = (char *)c->d_meta[0].p;
     auto *d_sptr = (unsigned long long *)mb;
     auto *d_dptr = d_sptr + M;
     auto *d_pin = (uint32_t *)(d_dptr + M);
     uint32_t *d_pout = d_pin + M, *d_tidx = d_pin + 2 * M;
     auto *d_tptr = (unsigned long long *)(mb + toff);
-    uint32_t *d_tcnt = (uint32_t *)(d_tptr + nt);
+    uint32_t *d_tcnt = (uint32_t *)(d_tptr + M);
     const double *d_sh = (const double *)c->d_shift[0].p;
-    if ((e = cudaMemcpyAsync(d_sptr, sptr.data(), M * 8, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemcpyAsync(d_dptr, dptr.data(), M * 8, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemcpyAsync(d_pin, pin.data(), M * 4, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemcpyAsync(d_pout, pout.data(), M * 4, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemcpyAsync(d_tidx, tidx.data(), M * 4, cudaMemcpyHostToDevice, s)) ||
-        (e = cudaMemcpyAsync((void *)d_sh, sh.data(), M * 3 * sizeof(double), cudaMemcpyHostToDevice, s)))
+    if ((e = cudaMemcpyAsync(mb, hm, M * 28, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync((void *)d_sh, ent.shift, M * 3 * sizeof(double), cudaMemcpyHostToDevice, s)))
         return cuda_fail(c, e, "host-to-device copy");
     if (c->pageable_access) {
         // The GPU reads the source solids and updates the target solids where
@@ -893,8 +859,8 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
         } else {
             // repeated targets: sums per target in device slots (atomics),
             // then one read-modify-write of each host target
-            if ((e = cudaMemcpyAsync(d_tptr, tptr.data(), nt * 8, cudaMemcpyHostToDevice, s)) ||
-                (e = cudaMemcpyAsync(d_tcnt, tcnt.data(), nt * 4, cudaMemcpyHostToDevice, s)))
+            if ((e = cudaMemcpyAsync(d_tptr, ent.tptr, nt * 8, cudaMemcpyHostToDevice, s)) ||
+                (e = cudaMemcpyAsync(d_tcnt, ent.tcnt, nt * 4, cudaMemcpyHostToDevice, s)))
                 return cuda_fail(c, e, "host-to-device copy");
             if ((e = c->d_dst[0].ensure(nt * stride * es)) || (e = cudaMemsetAsync(c->d_dst[0].p, 0, nt * stride * es, s)))
                 return cuda_fail(c, e, "device buffers");
@@ -932,7 +898,8 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
     };
     parallel(M, [&](size_t lo, size_t hi) {
         for (size_t k = lo; k < hi; ++k)
-            std::memcpy(hs + k * stride * es, (const void *)(uintptr_t)sptr[k], (size_t)pin[k] * (pin[k] + 1) * es);
+            std::memcpy(hs + k * stride * es, (const void *)(uintptr_t)ent.sptr[k],
+                        (size_t)ent.pin[k] * (ent.pin[k] + 1) * es);
     });
     if ((e = cudaMemcpyAsync(c->d_src[0].p, hs, M * stride * es, cudaMemcpyHostToDevice, s)) ||
         (e = cudaMemsetAsync(c->d_dst[0].p, 0, nt * stride * es, s)))
@@ -948,13 +915,13 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
     parallel(nt, [&](size_t lo, size_t hi) {
         for (size_t j = lo; j < hi; ++j) {
             if (c->dtype == SFMM_F64) {
-                double *o = (double *)(uintptr_t)tptr[j];
+                double *o = (double *)(uintptr_t)ent.tptr[j];
                 const double *r = (const double *)(hd + j * stride * es);
-                for (size_t q = 0; q < tcnt[j]; ++q) o[q] += r[q];
+                for (size_t q = 0; q < ent.tcnt[j]; ++q) o[q] += r[q];
             } else {
-                float *o = (float *)(uintptr_t)tptr[j];
+                float *o = (float *)(uintptr_t)ent.tptr[j];
                 const float *r = (const float *)(hd + j * stride * es);
-                for (size_t q = 0; q < tcnt[j]; ++q) o[q] += r[q];
+                for (size_t q = 0; q < ent.tcnt[j]; ++q) o[q] += r[q];
             }
         }
     });

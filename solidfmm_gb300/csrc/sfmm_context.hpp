@@ -14,6 +14,7 @@
 #include <utility>
 #include <vector>
 
+#include "sfmm_hostbatch.hpp"
 #include "sfmm_launch.hpp"
 #include "sfmm_tables.hpp"
 
@@ -90,6 +91,7 @@ struct sfmm_context {
     std::map<std::pair<int, int>, sfmm::LaunchShape> shapes;  // (arith, order bound) -> launch shape
     int *d_woff = nullptr, *d_hoff = nullptr;            // table offsets (shared by all arithmetics)
     bool pageable_access = false;  // the GPU reads pageable host memory through the host page tables
+    sfmm::SlotScratch slot_scratch;  // target table of the classic host call
 };
 
 namespace sfmm {

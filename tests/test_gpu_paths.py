@@ -312,3 +312,44 @@ def test_classic_host_call_pointer_batches(native, oracle, pattern, prec):
             got[j, :c] = tgts[j][comp * c:(comp + 1) * c]
         tol = 1e-11 if prec == 0 else 1e-7
         assert rel_err(got - start, ref - start, norm_weights(12, "L")) < tol, comp
+
+
+@pytest.mark.parametrize("order", ["ascending", "runs", "shuffled", "descending"])
+def test_classic_host_call_target_orders(native, oracle, order):
+    """sfmm_translate_host with targets that are rows of one array, named in
+    rising order (distinct), sorted with repeats (runs), in random order with
+    repeats, and in falling order (distinct): the host bookkeeping takes its
+    three slot paths and every result matches the oracle."""
+    import ctypes as C
+
+    L = native.load()
+    P, S = 10, 110
+    rng = np.random.default_rng({"ascending": 81, "runs": 82, "shuffled": 83, "descending": 84}[order])
+    n = 3000
+    b = _batch("m2l", (1, P), P, n, 85)  # seeded P2M sources and shifts; targets arranged below
+    src, pin, xyz = b["src"], b["Pin"].astype(np.int64), b["xyz"]
+    sidx = np.arange(n)
+    if order in ("ascending", "descending"):
+        tidx = np.arange(n) if order == "ascending" else np.arange(n)[::-1].copy()
+        nt = n
+    else:
+        tidx = np.sort(rng.integers(0, 400, size=n))
+        nt = 400
+        if order == "shuffled":
+            rng.shuffle(tidx)
+    dst = rng.normal(size=(nt, S)) * 1e-3
+    start = dst.copy()
+    ctx = native.Context(P, "f64")
+    sp = (C.c_void_p * n)(*[src.ctypes.data + int(sidx[i]) * S * 8 for i in range(n)])
+    dp = (C.c_void_p * n)(*[dst.ctypes.data + int(tidx[i]) * S * 8 for i in range(n)])
+    cin = (C.c_size_t * n)(*[int(v) for v in pin])
+    cout = (C.c_size_t * n)(*([P] * n))
+    x, y, z = (np.ascontiguousarray(xyz[:, k]) for k in range(3))
+    L.sfmm_translate_host.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p]
+    rc = L.sfmm_translate_host(ctx.h, 1, 0, n, sp, cin, dp, cout, 1, x.ctypes.data, y.ctypes.data, z.ctypes.data)
+    assert rc == 0, L.sfmm_last_error(ctx.h)
+    ref = start.copy()
+    oracle.naive("m2l", src, pin.astype(np.uint32), ref, np.full(n, P, np.uint32), xyz,
+                 sidx=sidx.astype(np.uint32), tidx=tidx.astype(np.uint32))
+    assert rel_err(dst - start, ref - start, norm_weights(P, "L")) < 1e-11
