@@ -4,33 +4,12 @@
 
 #include <algorithm>
 #include <cstring>
-#include <thread>
 
 namespace sfmm {
 
 namespace {
 
-// fn(t) for t in [0, nthr), t = 0 on the calling thread
-template <class F>
-void fork_join(size_t nthr, F &&fn)
-{
-    if (nthr <= 1) {
-        fn(size_t(0));
-        return;
-    }
-    std::vector<std::thread> th;
-    th.reserve(nthr - 1);
-    try {
-        for (size_t t = 1; t < nthr; ++t) th.emplace_back(fn, t);
-    } catch (...) {
-        for (auto &x : th) x.join();
-        throw;
-    }
-    fn(size_t(0));
-    for (auto &x : th) x.join();
-}
-
-inline size_t lo_of(size_t n, size_t t, size_t nthr) { return n * t / nthr; }
+inline size_t lo_of(size_t n, size_t t, size_t nthr) { return share_lo(n, t, nthr); }
 
 // relaxed atomic max of a 32-bit counter
 inline void atomic_max(uint32_t *p, uint32_t v)

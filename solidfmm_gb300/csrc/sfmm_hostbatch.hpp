@@ -17,9 +17,33 @@
 #include <cstddef>
 #include <cstdint>
 #include <memory>
+#include <thread>
 #include <vector>
 
 namespace sfmm {
+
+// fn(t) for every share t in [0, nthr): share 0 on the calling thread, the
+// others on new threads; shares whose thread cannot be created run on the
+// calling thread, so this never throws on its own.
+template <class F>
+void fork_join(size_t nthr, F &&fn)
+{
+    std::vector<std::thread> th;
+    size_t spawned = 1;
+    if (nthr > 1) {
+        try {
+            th.reserve(nthr - 1);
+            for (; spawned < nthr; ++spawned) th.emplace_back(fn, spawned);
+        } catch (...) {
+        }
+    }
+    fn(size_t(0));
+    for (size_t t = spawned; t < nthr; ++t) fn(t);
+    for (auto &x : th) x.join();
+}
+
+// first index of share t of n items split nthr ways
+inline size_t share_lo(size_t n, size_t t, size_t nthr) { return n * t / nthr; }
 
 struct ClassicInput {
     size_t n = 0;                      // translations
@@ -71,7 +95,7 @@ ClassicScan classic_scan(const ClassicInput &in, size_t nthr);
 
 // Fill the entries and slots with the scan's threads; returns the slot
 // count.  *repeat is whether a target address is named by more than one
-// entry.  Throws std::bad_alloc or std::system_error (thread creation).
+// entry.  Throws std::bad_alloc (table growth).
 size_t classic_fill(const ClassicInput &in, const ClassicScan &sc, const ClassicEntries &out, SlotScratch &scratch,
                     bool *repeat, SlotPath *path = nullptr);
 

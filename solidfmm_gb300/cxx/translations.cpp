@@ -12,6 +12,7 @@
 #include <solidfmm/threadlocal_buffer.hpp>
 #include <solidfmm/translations.hpp>
 
+#include <cstdint>
 #include <cstdio>
 #include <exception>
 #include <memory>
@@ -20,6 +21,7 @@
 #include <vector>
 
 #include "sfmm.h"
+#include "sfmm_hostbatch.hpp"
 
 namespace solidfmm
 {
@@ -45,27 +47,28 @@ struct batch {
     std::vector<size_t> pin, pout;
     std::vector<real> x, y, z;
 
-    void reserve(size_t n)
+    void resize(size_t m)
     {
-        src.reserve(n);
-        dst.reserve(n);
-        pin.reserve(n);
-        pout.reserve(n);
-        x.reserve(n);
-        y.reserve(n);
-        z.reserve(n);
+        src.resize(m);
+        dst.resize(m);
+        pin.resize(m);
+        pout.resize(m);
+        x.resize(m);
+        y.resize(m);
+        z.resize(m);
     }
-    void add(const solid<real> &s, solid<real> &t, real xx, real yy, real zz)
+    // the components of one (source, target) pair at positions k, k+1, ...
+    void put(size_t k, const solid<real> &s, solid<real> &t, real xx, real yy, real zz)
     {
         const size_t Si = s.order() * (s.order() + 1), So = t.order() * (t.order() + 1);
-        for (size_t d = 0; d < s.dimension(); ++d) {
-            src.push_back(s.memptr() + d * Si);
-            dst.push_back(t.memptr() + d * So);
-            pin.push_back(s.order());
-            pout.push_back(t.order());
-            x.push_back(xx);
-            y.push_back(yy);
-            z.push_back(zz);
+        for (size_t d = 0; d < s.dimension(); ++d, ++k) {
+            src[k] = s.memptr() + d * Si;
+            dst[k] = t.memptr() + d * So;
+            pin[k] = s.order();
+            pout[k] = t.order();
+            x[k] = xx;
+            y[k] = yy;
+            z[k] = zz;
         }
     }
     int run(sfmm_context *ctx, int op) const
@@ -74,6 +77,14 @@ struct batch {
         return sfmm_translate_host(ctx, op, prec, src.size(), src.data(), pin.data(), dst.data(), pout.data(), 1,
                                    x.data(), y.data(), z.data());
     }
+};
+
+// One translation of a call: source, target, shift.
+template <typename real>
+struct pair_ref {
+    const solid<real> *s;
+    solid<real> *t;
+    real x, y, z;
 };
 
 const char *op_name(int op) { return op == SFMM_M2M ? "m2m" : (op == SFMM_M2L ? "m2l" : "l2l"); }
@@ -94,22 +105,61 @@ void raise(sfmm_context *ctx, int rc, int op, const char *type)
 }
 
 template <typename real>
-void check_pair(const operator_data<real> &op, const solid<real> &s, const solid<real> &t, int opk)
-{
-    if (s.dimension() != t.dimension())
-        throw std::logic_error{std::string{"solidfmm::"} + op_name(opk) + "<" + kind<real>::name +
-                               ">(): dimension mismatch."};
-    if (s.order() > op.order() || t.order() > op.order())
-        throw std::out_of_range{std::string{"solidfmm::"} + op_name(opk) + "<" + kind<real>::name +
-                                ">(): orders exceeding operator data."};
-}
-
-template <typename real>
 void check_buffer(const operator_data<real> &op, const threadlocal_buffer<real> &buf, int opk)
 {
     if (!buf.compatible(op))
         throw std::logic_error{std::string{"solidfmm::"} + op_name(opk) + "<" + kind<real>::name +
                                ">(): operator data and buffer incompatible"};
+}
+
+// Check (when asked) and gather the n translations pair(i) of a call into a
+// batch, on the host cores in parallel: each share of the translations counts
+// its components, then writes its own range.  An invalid pair throws the
+// exception a sequential loop would throw first (dimension checked before
+// orders, lowest index first).
+template <typename real, class Pair>
+void gather(int opk, const operator_data<real> &op, size_t n, Pair &&pair, bool checked, batch<real> &b)
+{
+    const size_t nthr = sfmm::host_threads(n);
+    std::vector<size_t> cnt(nthr, 0), bad(nthr, SIZE_MAX);
+    std::vector<int> why(nthr, 0);
+    sfmm::fork_join(nthr, [&](size_t t) {
+        size_t c = 0;
+        for (size_t i = sfmm::share_lo(n, t, nthr); i < sfmm::share_lo(n, t + 1, nthr); ++i) {
+            const pair_ref<real> r = pair(i);
+            if (checked) {
+                if (r.s->dimension() != r.t->dimension()) {
+                    bad[t] = i;
+                    why[t] = 1;
+                    break;
+                }
+                if (r.s->order() > op.order() || r.t->order() > op.order()) {
+                    bad[t] = i;
+                    why[t] = 2;
+                    break;
+                }
+            }
+            c += r.s->dimension();
+        }
+        cnt[t] = c;
+    });
+    for (size_t t = 0; t < nthr; ++t) {
+        if (bad[t] == SIZE_MAX) continue;
+        const std::string where = std::string{"solidfmm::"} + op_name(opk) + "<" + kind<real>::name + ">(): ";
+        if (why[t] == 1) throw std::logic_error{where + "dimension mismatch."};
+        throw std::out_of_range{where + "orders exceeding operator data."};
+    }
+    std::vector<size_t> off(nthr + 1, 0);
+    for (size_t t = 0; t < nthr; ++t) off[t + 1] = off[t] + cnt[t];
+    b.resize(off[nthr]);
+    sfmm::fork_join(nthr, [&](size_t t) {
+        size_t k = off[t];
+        for (size_t i = sfmm::share_lo(n, t, nthr); i < sfmm::share_lo(n, t + 1, nthr); ++i) {
+            const pair_ref<real> r = pair(i);
+            b.put(k, *r.s, *r.t, r.x, r.y, r.z);
+            k += r.s->dimension();
+        }
+    });
 }
 
 template <typename real>
@@ -118,10 +168,8 @@ void classic(int opk, const operator_data<real> &op, threadlocal_buffer<real> &b
              const real *z)
 {
     check_buffer(op, buf, opk);
-    for (size_t i = 0; i < howmany; ++i) check_pair(op, *M[i], *L[i], opk);
     batch<real> b;
-    b.reserve(howmany);
-    for (size_t i = 0; i < howmany; ++i) b.add(*M[i], *L[i], x[i], y[i], z[i]);
+    gather(opk, op, howmany, [&](size_t i) { return pair_ref<real>{M[i], L[i], x[i], y[i], z[i]}; }, true, b);
     int rc = b.run(op.context(), opk);
     if (rc) raise(op.context(), rc, opk, kind<real>::name);
 }
@@ -130,11 +178,10 @@ template <typename real>
 void items(int opk, const operator_data<real> &op, const translation_info<real> *begin,
            const translation_info<real> *end, bool checked)
 {
-    if (checked)
-        for (auto *i = begin; i != end; ++i) check_pair(op, *i->source, *i->target, opk);
     batch<real> b;
-    b.reserve(size_t(end - begin));
-    for (auto *i = begin; i != end; ++i) b.add(*i->source, *i->target, i->x, i->y, i->z);
+    gather(opk, op, size_t(end - begin),
+           [&](size_t i) { return pair_ref<real>{begin[i].source, begin[i].target, begin[i].x, begin[i].y, begin[i].z}; },
+           checked, b);
     int rc = b.run(op.context(), opk);
     if (rc) {
         if (checked) raise(op.context(), rc, opk, kind<real>::name);
