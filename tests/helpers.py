@@ -95,3 +95,53 @@ def run_device(ctx, op, precision, src, dst0, Pin, Pout, xyz, sidx=None, tidx=No
     torch.cuda.synchronize()
     assert ctx.device_status() == 0
     return d.cpu().numpy()
+
+
+def device_batch(ctx, op, P, N, nq, seed, dev):
+    """Full-size inputs generated on the GPU (the benchmark's distribution):
+    sources by P2M (P2L for L2L) of nq unit charges of random sign uniform in
+    a ball of radius 0.5, the L2L clouds centred at distance U[2,4]; M2L
+    shifts of uniform direction and length U[2,4], M2M/L2L shifts to a random
+    octant corner (length 0.5 sqrt 3)."""
+    import torch
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    S = P * (P + 1)
+    src = torch.zeros(N, S, dtype=torch.float64, device=dev)
+    for b in range(0, N, 250_000):
+        m = min(250_000, N - b)
+        d = torch.randn(m, nq, 3, dtype=torch.float64, device=dev, generator=g)
+        pos = d / d.norm(dim=2, keepdim=True) * 0.5 * torch.rand(m, nq, 1, dtype=torch.float64, device=dev,
+                                                                 generator=g) ** (1.0 / 3.0)
+        q = torch.randint(0, 2, (m, nq), device=dev, generator=g).to(torch.float64) * 2 - 1
+        if op == "l2l":
+            u = torch.randn(m, 3, dtype=torch.float64, device=dev, generator=g)
+            pos = pos + (u / u.norm(dim=1, keepdim=True) *
+                         (2 + 2 * torch.rand(m, 1, dtype=torch.float64, device=dev, generator=g)))[:, None, :]
+        ctx.p2x(1 if op == "l2l" else 0, m, nq, q.contiguous(), pos.contiguous(),
+                torch.zeros(m, 3, dtype=torch.float64, device=dev), src[b:b + m], S)
+    if op == "m2l":
+        u = torch.randn(N, 3, dtype=torch.float64, device=dev, generator=g)
+        shift = u / u.norm(dim=1, keepdim=True) * (2 + 2 * torch.rand(N, 1, dtype=torch.float64, device=dev,
+                                                                      generator=g))
+    else:
+        shift = 0.5 * (torch.randint(0, 2, (N, 3), device=dev, generator=g).to(torch.float64) * 2 - 1)
+    return src, shift.contiguous()
+
+
+def rel_err_dev(got, ref, weights=None):
+    """rel_err on device tensors (max over rows of the relative L2 error),
+    reduced on the GPU; rows with a zero reference are skipped."""
+    import torch
+
+    got = got.to(torch.float64)
+    ref = ref.to(torch.float64)
+    if weights is not None:
+        w = torch.as_tensor(weights[: got.shape[-1]], dtype=torch.float64, device=got.device)
+        got = got * w
+        ref = ref * w
+    num = (got - ref).norm(dim=-1)
+    den = ref.norm(dim=-1)
+    ok = den > 0
+    return float((num[ok] / den[ok]).max()) if bool(ok.any()) else float(num.max())
