@@ -82,14 +82,20 @@ int ensure_tables(sfmm_context *c, Arith a)
     DevTables &t = c->tab[(int)a];
     if (t.ready) return SFMM_OK;
     cudaError_t e;
+    const size_t n8 = c->host.woff8.size();
     if (!c->d_woff) {
         if ((e = cudaMalloc(&c->d_woff, sizeof(int) * c->P)) != cudaSuccess ||
             (e = cudaMalloc(&c->d_hoff, sizeof(int) * c->P)) != cudaSuccess ||
             (e = cudaMemcpy(c->d_woff, c->host.woff.data(), sizeof(int) * c->P, cudaMemcpyHostToDevice)) != cudaSuccess ||
             (e = cudaMemcpy(c->d_hoff, c->host.hoff.data(), sizeof(int) * c->P, cudaMemcpyHostToDevice)) != cudaSuccess)
             return cuda_fail(c, e, "table upload");
+        if (n8 && ((e = cudaMalloc(&c->d_woff8, sizeof(int) * n8)) != cudaSuccess ||
+                   (e = cudaMemcpy(c->d_woff8, c->host.woff8.data(), sizeof(int) * n8, cudaMemcpyHostToDevice)) !=
+                       cudaSuccess))
+            return cuda_fail(c, e, "table upload");
     }
     if ((e = upload(&t.W, c->host.W, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+    if (n8 && (e = upload(&t.W8, c->host.W8, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
     if ((e = upload(&t.ein_M, c->host.e_in_M, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
     if ((e = upload(&t.ein_L, c->host.e_in_L, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
     if ((e = upload(&t.eout_L, c->host.e_out_L, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
@@ -98,11 +104,15 @@ int ensure_tables(sfmm_context *c, Arith a)
         if ((e = upload(&t.H[k], c->host.H[k], a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
     if (a == Arith::FFQ) {
         // |w| <= 1 (orthogonal matrices): round(w 2^30) fits int32
-        std::vector<int32_t> q(c->host.W.size());
-        for (size_t i = 0; i < q.size(); ++i) q[i] = (int32_t)std::llround(std::ldexp(c->host.W[i], 30));
-        if ((e = cudaMalloc(&t.Wq, q.size() * sizeof(int32_t) + 16)) != cudaSuccess ||
-            (e = cudaMemcpy(t.Wq, q.data(), q.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess)
-            return cuda_fail(c, e, "table upload");
+        auto upload_q30 = [](void **dst, const std::vector<double> &W) {
+            std::vector<int32_t> q(W.size());
+            for (size_t i = 0; i < q.size(); ++i) q[i] = (int32_t)std::llround(std::ldexp(W[i], 30));
+            cudaError_t err = cudaMalloc(dst, q.size() * sizeof(int32_t) + 16);
+            if (err == cudaSuccess) err = cudaMemcpy(*dst, q.data(), q.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+            return err;
+        };
+        if ((e = upload_q30(&t.Wq, c->host.W)) != cudaSuccess) return cuda_fail(c, e, "table upload");
+        if (n8 && (e = upload_q30(&t.Wq8, c->host.W8)) != cudaSuccess) return cuda_fail(c, e, "table upload");
     }
     t.ready = true;
     return SFMM_OK;
@@ -110,7 +120,7 @@ int ensure_tables(sfmm_context *c, Arith a)
 
 void free_tables(DevTables &t)
 {
-    void *ps[] = {t.W, t.ein_M, t.ein_L, t.eout_L, t.eout_M, t.H[0], t.H[1], t.H[2], t.Wq};
+    void *ps[] = {t.W, t.ein_M, t.ein_L, t.eout_L, t.eout_M, t.H[0], t.H[1], t.H[2], t.Wq, t.W8, t.Wq8};
     for (void *p : ps)
         if (p) cudaFree(p);
     t = DevTables{};
@@ -189,6 +199,8 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
               const unsigned long long *dst_ptr)
 {
     if (n == 0) return SFMM_OK;
+    static const char *const kName[3] = {"sfmm m2m launch", "sfmm m2l launch", "sfmm l2l launch"};
+    Range range(kName[(op >= SFMM_M2M && op <= SFMM_L2L) ? op - SFMM_M2M : 1]);
     a = resolve_arith(a, op, Pbound);
     if (Pbound < 1) Pbound = 1;
     LaunchShape s;
@@ -217,9 +229,12 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.src_ptr = src_ptr;
     p.dst_ptr = dst_ptr;
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
-    p.W = t.W;
-    p.Wq = static_cast<const int *>(t.Wq);
-    p.woff = c->d_woff;
+    // swap blocks padded for this launch's group size (4 or 8 threads per
+    // translation step 8 rows, one warp 32)
+    const bool w8 = s.G != 32 && c->d_woff8;
+    p.W = w8 ? t.W8 : t.W;
+    p.Wq = static_cast<const int *>(w8 ? t.Wq8 : t.Wq);
+    p.woff = w8 ? c->d_woff8 : c->d_woff;
     p.hoff = c->d_hoff;
     p.rowpad = c->host.pad;
     p.ein = (op == SFMM_L2L) ? t.ein_L : t.ein_M;
@@ -406,6 +421,7 @@ void sfmm_destroy(sfmm_context *c)
     c->d_work.release();
     if (c->d_status) cudaFree(c->d_status);
     if (c->d_woff) cudaFree(c->d_woff);
+    if (c->d_woff8) cudaFree(c->d_woff8);
     if (c->d_hoff) cudaFree(c->d_hoff);
     c->h_src.release();
     c->h_dst.release();
@@ -608,6 +624,7 @@ int sfmm_device_status(sfmm_context *c, int *flags)
 int sfmm_bucket_by_order(sfmm_context *c, size_t n, const uint32_t *p_in, const uint32_t *p_out, uint32_t *order)
 {
     if (!c) return SFMM_INVALID_ARG;
+    Range range("sfmm bucket");
     if (n == 0) return SFMM_OK;
     if (!p_in || !p_out || !order) return fail(c, SFMM_INVALID_ARG, "null device pointer");
     cudaSetDevice(c->device);
@@ -623,6 +640,7 @@ int sfmm_p2x_device(sfmm_context *c, int kind, size_t nexp, size_t nq, const dou
                     const double *centre, void *out, size_t out_stride)
 {
     if (!c) return SFMM_INVALID_ARG;
+    Range range("sfmm p2m/p2l");
     if (kind != 0 && kind != 1) return fail(c, SFMM_INVALID_ARG, "kind must be 0 (P2M) or 1 (P2L)");
     if (nexp == 0) return SFMM_OK;
     if (!charge || !pos || !centre || !out) return fail(c, SFMM_INVALID_ARG, "null device pointer");
@@ -640,6 +658,7 @@ int sfmm_eval_device(sfmm_context *c, int kind, size_t npts, const double *pos, 
                      double *gradient)
 {
     if (!c) return SFMM_INVALID_ARG;
+    Range range("sfmm l2p/m2p");
     if (kind != 0 && kind != 1) return fail(c, SFMM_INVALID_ARG, "kind must be 0 (L2P) or 1 (M2P)");
     if (npts == 0) return SFMM_OK;
     if (!pos || !E || !centre || !potential) return fail(c, SFMM_INVALID_ARG, "null device pointer");
@@ -660,6 +679,7 @@ int sfmm_translate_host_packed(sfmm_context *c, int op, int precision, size_t n,
                                const uint32_t *p_out, const double *shift, int flags)
 {
     if (!c) return SFMM_INVALID_ARG;
+    Range range("sfmm host packed call");
     if (op < SFMM_M2M || op > SFMM_L2L) return fail(c, SFMM_INVALID_ARG, "unknown operator %d", op);
     Arith a;
     int st = arith_of(c, precision, &a);
@@ -768,6 +788,7 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
                         const void *z)
 {
     if (!c) return SFMM_INVALID_ARG;
+    Range range("sfmm host call");
     if (op < SFMM_M2M || op > SFMM_L2L) return fail(c, SFMM_INVALID_ARG, "unknown operator %d", op);
     Arith a;
     int st = arith_of(c, precision, &a);
@@ -831,6 +852,7 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
     bool repeat = false;
     size_t nt = 0;
     try {
+        Range fill_range("sfmm host bookkeeping");
         nt = classic_fill(in, sc, ent, c->slot_scratch, &repeat);
     } catch (const std::bad_alloc &) {
         return fail(c, SFMM_OOM, "host bookkeeping");

@@ -5,6 +5,7 @@
 #include "sfmm.h"
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstdint>
@@ -24,6 +25,7 @@ struct DevTables {
     void *W = nullptr, *ein_M = nullptr, *ein_L = nullptr, *eout_L = nullptr, *eout_M = nullptr;
     void *H[3] = {nullptr, nullptr, nullptr};
     void *Wq = nullptr;  // Q1.30 swap matrices (fixed-point variant only)
+    void *W8 = nullptr, *Wq8 = nullptr;  // 8-row padded copies (HostTables::W8), contexts above order 32
     bool ready = false;
 };
 
@@ -90,11 +92,21 @@ struct sfmm_context {
     cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
     std::map<std::pair<int, int>, sfmm::LaunchShape> shapes;  // (arith, order bound) -> launch shape
     int *d_woff = nullptr, *d_hoff = nullptr;            // table offsets (shared by all arithmetics)
+    int *d_woff8 = nullptr;                              // offsets of the 8-row padded swap blocks
     bool pageable_access = false;  // the GPU reads pageable host memory through the host page tables
     sfmm::SlotScratch slot_scratch;  // target table of the classic host call
 };
 
 namespace sfmm {
+
+// NVTX range over a scope, shown by profilers on the host timeline (a no-op
+// unless a tool is attached)
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
 
 // record an error on the context and return the status
 int fail(sfmm_context *c, int st, const char *fmt, ...);

@@ -17,6 +17,7 @@ namespace sfmm {
 template <class A, int G, int ACC, bool FIX>
 static cudaError_t launch_inst(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
+    clear_stale_error();
     k_translate<A, G, ACC, FIX><<<grid, s.threads, s.smem, st>>>(p);
     return cudaGetLastError();
 }

@@ -8,6 +8,11 @@
 
 namespace sfmm {
 
+// Clear a stale, non-sticky error that an earlier failed runtime call on this
+// thread left behind (a failed allocation, the library's or the caller's), so
+// that the cudaGetLastError after a launch reports that launch alone.
+inline void clear_stale_error() { (void)cudaGetLastError(); }
+
 struct KParams;
 
 // FFQ: float-float with block fixed-point swaps and beta rotations

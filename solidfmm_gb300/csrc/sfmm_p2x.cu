@@ -109,6 +109,7 @@ cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, 
     if (nexp == 0) return cudaSuccess;
     int tb = 128;
     long long grid = (nexp + tb - 1) / tb;
+    clear_stale_error();
     if (f64)
         k_p2x<double><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, q, pos, centre, (double *)out, stride);
     else
@@ -234,6 +235,7 @@ cudaError_t launch_eval(bool f64, int kind, int P, long long npts, const double 
     if (npts == 0) return cudaSuccess;
     const int tb = 128;
     const long long grid = (npts + tb - 1) / tb;
+    clear_stale_error();
     if (f64)
         k_eval<double><<<(unsigned)grid, tb, 0, st>>>(kind, P, npts, pos, box, (const double *)E, stride, centre,
                                                        pot, grad);
@@ -266,6 +268,7 @@ cudaError_t launch_add_slots(bool f64, long long nt, const unsigned long long *t
     if (nt == 0) return cudaSuccess;
     const int tb = 256;
     const long long grid = (nt * 32 + tb - 1) / tb;
+    clear_stale_error();
     if (f64)
         k_add_slots<double><<<(unsigned)grid, tb, 0, st>>>(nt, tptr, cnt, (const double *)slots, stride);
     else
@@ -327,6 +330,7 @@ cudaError_t launch_bucket(long long n, const uint32_t *pin, const uint32_t *pout
 {
     const int K = P + 1;
     const int nkeys = K * K;
+    clear_stale_error();
     cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t) * nkeys, st);
     if (e != cudaSuccess) return e;
     if (n == 0) return cudaSuccess;

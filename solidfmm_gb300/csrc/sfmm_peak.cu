@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "sfmm.h"
+#include "sfmm_launch.hpp"
 
 namespace {
 
@@ -62,6 +63,7 @@ extern "C" int sfmm_measure_imad_peak(int device, double *ops_per_second)
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
+    sfmm::clear_stale_error();
     for (int rep = 0; rep < 4; ++rep) {
         cudaEventRecord(e0);
         k_imad_peak<<<blocks, threads>>>((long long *)out, iters, 3, 5);
@@ -94,6 +96,7 @@ extern "C" int sfmm_measure_fma_peak(int fp64, int device, double *flops_per_sec
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
+    sfmm::clear_stale_error();
     for (int rep = 0; rep < 4; ++rep) {
         cudaEventRecord(e0);
         if (fp64) k_fma_peak<double><<<blocks, threads>>>((double *)out, iters, 0.999999, 1e-7);

@@ -201,6 +201,7 @@ int sfmm_plan_add(sfmm_plan *p, int op, int precision, size_t n, const void *src
 int sfmm_plan_finalize(sfmm_plan *p)
 {
     if (!p) return SFMM_INVALID_ARG;
+    Range range("sfmm plan finalize");
     sfmm_context *c = p->ctx;
     if (p->finalized) return fail(c, SFMM_INVALID_ARG, "plan already finalized");
     if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, SFMM_CUDA_ERROR, "cannot select device %d", c->device);
@@ -273,6 +274,7 @@ int sfmm_plan_finalize(sfmm_plan *p)
 int sfmm_plan_run(sfmm_plan *p)
 {
     if (!p) return SFMM_INVALID_ARG;
+    Range range("sfmm plan replay");
     sfmm_context *c = p->ctx;
     if (!p->finalized) return fail(c, SFMM_INVALID_ARG, "plan not finalized");
     cudaError_t e = cudaGraphLaunch(p->exec, c->stream);

@@ -1,5 +1,6 @@
 #include "sfmm_tables.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 
@@ -59,33 +60,28 @@ double w_entry(const HostTables &t, int n, int part, int i, int j)
     return t.W[t.woff[n] + size_t(j >> 1) * 2 * R + (part ? R : 0) + i];
 }
 
-HostTables build_tables(int P)
-{
-    HostTables t;
-    t.P = P;
-    const int pad = row_pad(P);
-    t.pad = pad;
-    auto B = swap_matrices(P);
-    SqrtFac sf(2 * P + 2);
-    std::vector<double> fac(2 * P + 2);
-    fac[0] = 1;
-    for (int k = 1; k < 2 * P + 2; ++k) fac[k] = fac[k - 1] * k;
-    const double s2 = std::sqrt(2.0);
+namespace {
 
-    t.woff.resize(P);
+// Swap blocks of degrees n < nmax with rows padded to a multiple of pad (the
+// layout of HostTables::W).
+void build_w(const std::vector<std::vector<double>> &B, const SqrtFac &sf, int nmax, int pad,
+             std::vector<double> &W, std::vector<int> &woff)
+{
+    const double s2 = std::sqrt(2.0);
+    woff.resize(nmax);
     size_t tot = 0;
-    for (int n = 0; n < P; ++n) {
-        t.woff[n] = (int)tot;
+    for (int n = 0; n < nmax; ++n) {
+        woff[n] = (int)tot;
         tot += 2 * size_t(wcols(n + 1)) * wrows(n + 1, pad);
     }
-    t.W.assign(tot, 0.0);
-    for (int n = 0; n < P; ++n) {
+    W.assign(tot, 0.0);
+    for (int n = 0; n < nmax; ++n) {
         const int d = n + 1, w = 2 * n + 1;
         auto Bv = [&](int m, int l) { return B[n][(m + n) + (l + n) * w]; };
         auto D = [&](int m) { return sf(n - m) * sf(n + m); };
         auto E = [&](int m) { return m == 0 ? D(0) / s2 : D(m); };
         const int R = wrows(d, pad);
-        double *WR = &t.W[t.woff[n]];  // slot t: W_R rows at 2tR, W_I rows at 2tR + R
+        double *WR = &W[woff[n]];  // slot t: W_R rows at 2tR, W_I rows at 2tR + R
         double *WI = WR + R;
         for (int i = 0; i < d; ++i)       // output row (coefficient m = i)
             for (int j = 0; j < d; ++j) { // input column (coefficient l = j)
@@ -103,6 +99,25 @@ HostTables build_tables(int P)
                 else if (i > 0 && j > 0) WI[slot] = imf * (D(i) / D(j));
             }
     }
+}
+
+}  // namespace
+
+HostTables build_tables(int P)
+{
+    HostTables t;
+    t.P = P;
+    const int pad = row_pad(P);
+    t.pad = pad;
+    auto B = swap_matrices(P);
+    SqrtFac sf(2 * P + 2);
+    std::vector<double> fac(2 * P + 2);
+    fac[0] = 1;
+    for (int k = 1; k < 2 * P + 2; ++k) fac[k] = fac[k - 1] * k;
+    const double s2 = std::sqrt(2.0);
+
+    build_w(B, sf, P, pad, t.W, t.woff);
+    if (pad != 8) build_w(B, sf, std::min(P, 32), 8, t.W8, t.woff8);
 
     size_t ne = size_t(P) * (P + 1) / 2;
     t.e_in_M.resize(ne);

@@ -35,6 +35,14 @@ struct HostTables {
     int pad = 8;
     std::vector<double> W;
     std::vector<int> woff;
+    // The kernels' swap loops step through a block with a compile-time row
+    // count: 8-row padding for 4 or 8 threads per translation (order bounds up
+    // to 32), 32-row padding for one warp per translation.  A context above
+    // order 32 (pad 32) therefore also keeps the blocks of degrees below 32
+    // padded to 8 rows, for its launches at order bounds up to 32; empty when
+    // pad is 8.
+    std::vector<double> W8;
+    std::vector<int> woff8;
     // Edge factors indexed n(n+1)/2 + m:
     std::vector<double> e_in_M;   // E^(n)_m        forward of M2M/M2L inputs
     std::vector<double> e_in_L;   // 1 / F^(n)_m    forward of L2L inputs

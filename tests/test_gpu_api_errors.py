@@ -1,6 +1,9 @@
 """Argument checking of the C ABI's newer entry points on a GPU context:
 evaluation, tuning and plans report errors through their status codes and
 leave their outputs untouched; empty plans run and launch nothing."""
+import os
+import sys
+
 import numpy as np
 import pytest
 
@@ -130,3 +133,43 @@ def test_concurrent_device_calls_share_a_context(native):
         ctx.translate_device("m2l", prec, n, src, S, n, d, S, n, o, o, sh, order_bound=bound)
         torch.cuda.synchronize()
         assert np.array_equal(out[i], d.cpu().numpy()), bound
+
+
+def test_device_allocation_failure_leaves_context_usable(native, oracle):
+    """A device allocation that cannot succeed (a tuning sample of 2^24
+    translations at P=86, about 1 TB) returns OOM; after each such failure
+    the same context still launches its kernels (P2M, bucketing, a
+    translation) and the result matches the oracle: the failed allocation's
+    error is not reported by a later launch."""
+    import torch
+
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import inputs
+    from helpers import norm_weights, rel_err, run_device
+
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(86, "f64")
+
+    def oom():
+        with pytest.raises(native.SfmmError, match="OOM"):
+            ctx.tune("m2l", 0, n=1 << 24)
+
+    oom()
+    q = torch.ones(1, 4, dtype=torch.float64, device=dev)
+    pos = torch.full((1, 4, 3), 0.1, dtype=torch.float64, device=dev)
+    out = torch.zeros(1, 86 * 87, dtype=torch.float64, device=dev)
+    ctx.p2x(0, 1, 4, q, pos, torch.zeros(1, 3, dtype=torch.float64, device=dev), out, 86 * 87)
+    torch.cuda.synchronize()
+    assert float(out[0, 0]) == 4.0  # R_0^0 = 1 per unit charge
+    oom()
+    o = torch.tensor([3, 1, 3, 2], dtype=torch.int32, device=dev)
+    perm = torch.zeros(4, dtype=torch.int32, device=dev)
+    ctx.bucket(4, o, o, perm)
+    torch.cuda.synchronize()
+    assert sorted(perm.cpu().tolist()) == [0, 1, 2, 3]
+    oom()
+    b = inputs.make_batch(np.random.default_rng(4), "m2l", 12, 12, 64, nq=16)
+    ref = b["dst"].copy()
+    oracle.naive("m2l", b["src"], b["Pin"], ref, b["Pout"], b["xyz"])
+    got = run_device(ctx, "m2l", 0, b["src"], b["dst"], b["Pin"], b["Pout"], b["xyz"], order_bound=12)
+    assert rel_err(got - b["dst"], ref - b["dst"], norm_weights(12, "L")) < 1e-12

@@ -353,3 +353,24 @@ def test_classic_host_call_target_orders(native, oracle, order):
     oracle.naive("m2l", src, pin.astype(np.uint32), ref, np.full(n, P, np.uint32), xyz,
                  sidx=sidx.astype(np.uint32), tidx=tidx.astype(np.uint32))
     assert rel_err(dst - start, ref - start, norm_weights(P, "L")) < 1e-11
+
+
+@pytest.mark.parametrize("P", [33, 86])
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["plain", "split", "split_ff"])
+def test_large_context_low_order_bounds(native, oracle, P, prec):
+    """A context above order 32 keeps its swap blocks padded for one warp per
+    translation; batches at order bounds up to 32 run the 4- and 8-thread
+    kernels, which step through 8-row padded copies.  All three operators at
+    bounds 5, 16 and 32 (28 for the split modes, their float-range limit;
+    mixed orders below each bound) against the oracle."""
+    ctx = native.Context(P, "f64")
+    for op in ("m2m", "m2l", "l2l"):
+        for bound in (5, 16, 32 if prec == 0 else 28):
+            b = _batch(op, (1, bound), (1, bound), 120, 300 + bound)
+            ref = _oracle(oracle, op, b)
+            got = run_device(ctx, op, prec, b["src"], b["dst"], b["Pin"], b["Pout"], b["xyz"], order_bound=bound)
+            w = norm_weights(bound, "M" if op == "m2m" else "L")
+            err = rel_err(got - b["dst"], ref - b["dst"], w)
+            # float-float: 1e-11 at low orders, the order-28 allowance of
+            # test_split_at_max_float_order above
+            assert err < {0: 1e-12, 1: 1e-7, 2: 1e-11 if bound <= 16 else 1e-8}[prec], (op, bound, err)
