@@ -374,3 +374,35 @@ def test_large_context_low_order_bounds(native, oracle, P, prec):
             # float-float: 1e-11 at low orders, the order-28 allowance of
             # test_split_at_max_float_order above
             assert err < {0: 1e-12, 1: 1e-7, 2: 1e-11 if bound <= 16 else 1e-8}[prec], (op, bound, err)
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["plain", "split", "split_ff"])
+def test_device_strides_wider_than_expansions(native, ctx64, oracle, prec):
+    """Expansions laid out with strides wider than P(P+1) and not a multiple
+    of 16 bytes apart (source stride S+13, target stride S+5 doubles),
+    gathered through index arrays with repeated targets: the padding is
+    neither read into a translation nor written."""
+    import torch
+
+    P = 14
+    S = P * (P + 1)
+    b = _batch("m2l", (1, P), (1, P), 300, 91, pattern="repeat")
+    ref = _oracle(oracle, "m2l", b)
+    dev = torch.device("cuda", 0)
+    ns, nt = b["src"].shape[0], b["dst"].shape[0]
+    src = np.full((ns, S + 13), np.nan)
+    src[:, :S] = b["src"]
+    dst = np.full((nt, S + 5), 7.0)
+    dst[:, :S] = b["dst"]
+    ts, td = torch.as_tensor(src, device=dev), torch.as_tensor(dst, device=dev)
+    i32 = lambda a: torch.as_tensor(np.asarray(a, np.uint32).astype(np.int32), device=dev)
+    ctx64.translate_device("m2l", prec, len(b["Pin"]), ts, S + 13, ns, td, S + 5, nt, i32(b["Pin"]), i32(b["Pout"]),
+                           torch.as_tensor(b["xyz"], device=dev), src_index=i32(b["sidx"]),
+                           dst_index=i32(b["tidx"]), repeat=True, order_bound=P)
+    torch.cuda.synchronize()
+    got = td.cpu().numpy()
+    assert np.all(got[:, S:] == 7.0)
+    # the sources' padding is NaN: a read of it would poison the targets
+    w = norm_weights(P, "L")
+    tol = {0: 1e-12, 1: 1e-7, 2: 1e-11}[prec]
+    assert rel_err(got[:, :S] - b["dst"], ref - b["dst"], w) < tol
