@@ -39,7 +39,9 @@ template <> struct kind<double> {
     static constexpr const char *name = "double";
 };
 
-// One batch of component translations in the C ABI's host form.
+// One batch of component translations in the C ABI's host form.  Each host
+// thread keeps its batch between calls (scratch()), so a call of the same
+// size as the last one neither allocates nor clears its arrays.
 template <typename real>
 struct batch {
     std::vector<const void *> src;
@@ -76,6 +78,11 @@ struct batch {
         const int prec = (g_split && sizeof(real) == sizeof(double)) ? SFMM_SPLIT : SFMM_PLAIN;
         return sfmm_translate_host(ctx, op, prec, src.size(), src.data(), pin.data(), dst.data(), pout.data(), 1,
                                    x.data(), y.data(), z.data());
+    }
+    static batch &scratch()
+    {
+        static thread_local batch b;
+        return b;
     }
 };
 
@@ -168,7 +175,7 @@ void classic(int opk, const operator_data<real> &op, threadlocal_buffer<real> &b
              const real *z)
 {
     check_buffer(op, buf, opk);
-    batch<real> b;
+    batch<real> &b = batch<real>::scratch();
     gather(opk, op, howmany, [&](size_t i) { return pair_ref<real>{M[i], L[i], x[i], y[i], z[i]}; }, true, b);
     int rc = b.run(op.context(), opk);
     if (rc) raise(op.context(), rc, opk, kind<real>::name);
@@ -178,7 +185,7 @@ template <typename real>
 void items(int opk, const operator_data<real> &op, const translation_info<real> *begin,
            const translation_info<real> *end, bool checked)
 {
-    batch<real> b;
+    batch<real> &b = batch<real>::scratch();
     gather(opk, op, size_t(end - begin),
            [&](size_t i) { return pair_ref<real>{begin[i].source, begin[i].target, begin[i].x, begin[i].y, begin[i].z}; },
            checked, b);
