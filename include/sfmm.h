@@ -210,11 +210,6 @@ int sfmm_bucket_by_order(sfmm_context *ctx, size_t n, const uint32_t *p_in, cons
 int sfmm_bucket_by_order_noalloc(size_t n, const uint32_t *p_in, const uint32_t *p_out, uint32_t *order,
                                  size_t max_order, void *stream);
 
-/* P2M / P2L on the device (the reference's fmadd(q, harmonics::R/S(P, x-c), E),
- * solid.cpp:70-104 with harmonics.cpp:32-80,177-224): for expansion j,
- *   out[j] += sum_{k<nq} charge[j*nq+k] * R(pos[j*nq+k] - centre[j])   (kind 0)
- *   out[j] += sum_{k<nq} charge[j*nq+k] * S(pos[j*nq+k] - centre[j])   (kind 1)
- * FP64 arithmetic; out has the context's data type and order P. */
 /* L2P / M2P on the device: for point j with expansion b = box[j] (box NULL:
  * b = j; nexp expansions addressable at `stride` reals, centres FP64),
  *   potential[j] += dot(E[b], R(pos[j] - centre[b]))    (kind 0, local)
@@ -226,8 +221,20 @@ int sfmm_eval_device(sfmm_context *ctx, int kind, size_t npts, const double *pos
                      const void *E, size_t stride, size_t nexp, const double *centre, double *potential,
                      double *gradient);
 
+/* P2M / P2L on the device (the reference's fmadd(q, harmonics::R/S(P, x-c), E),
+ * solid.cpp:70-104 with harmonics.cpp:32-80,177-224): for expansion j,
+ *   out[j] += sum_{k<nq} charge[j*nq+k] * R(pos[j*nq+k] - centre[j])   (kind 0)
+ *   out[j] += sum_{k<nq} charge[j*nq+k] * S(pos[j*nq+k] - centre[j])   (kind 1)
+ * FP64 arithmetic; out has the context's data type and order P. */
 int sfmm_p2x_device(sfmm_context *ctx, int kind, size_t nexp, size_t nq, const double *charge,
                     const double *pos, const double *centre, void *out, size_t out_stride);
+
+/* The same with ragged particle sets (leaves of a tree with their particles
+ * sorted by leaf): expansion j takes particles k in [offset[j], offset[j+1])
+ * (offset: nexp + 1 non-decreasing device values; not range-checked). */
+int sfmm_p2x_ragged_device(sfmm_context *ctx, int kind, size_t nexp, const uint32_t *offset,
+                           const double *charge, const double *pos, const double *centre, void *out,
+                           size_t out_stride);
 
 /* Diagnostics: measured FMA-pipe throughput (flop/s, 2 per FMA) of the
  * device, FP64 (fp64 = 1) or FP32 (fp64 = 0); the roofline denominator of

@@ -29,6 +29,7 @@ EXPORTS = [
     "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak", "sfmm_bucket_by_order_noalloc",
     "sfmm_set_group", "sfmm_tune", "sfmm_plan_create", "sfmm_plan_add", "sfmm_plan_finalize", "sfmm_plan_run",
     "sfmm_plan_launches", "sfmm_plan_segments", "sfmm_plan_destroy", "sfmm_eval_device", "sfmm_bounding_sphere",
+    "sfmm_p2x_ragged_device",
 ]
 
 
@@ -76,6 +77,7 @@ def load():
     L.sfmm_translate_host.argtypes = [vp, C.c_int, C.c_int, sz, vp, vp, vp, vp, sz, vp, vp, vp]
     L.sfmm_bucket_by_order.argtypes = [vp, sz, u32p, u32p, u32p]
     L.sfmm_p2x_device.argtypes = [vp, C.c_int, sz, sz, dp, dp, dp, vp, sz]
+    L.sfmm_p2x_ragged_device.argtypes = [vp, C.c_int, sz, u32p, dp, dp, dp, vp, sz]
     L.sfmm_launch_count.argtypes = [vp]
     L.sfmm_launch_count.restype = C.c_uint64
     L.sfmm_host_table.argtypes = [sz, C.c_int, C.c_int, vp, sz, C.POINTER(C.c_size_t)]
@@ -234,6 +236,12 @@ class Context:
     def p2x(self, kind, nexp, nq, charge, pos, centre, out, out_stride):
         self._check(self.L.sfmm_p2x_device(self.h, kind, nexp, nq, _ptr(charge), _ptr(pos), _ptr(centre),
                                            _ptr(out), out_stride))
+
+    def p2x_ragged(self, kind, nexp, offset, charge, pos, centre, out, out_stride):
+        """P2M (kind 0) / P2L (kind 1) with expansion j taking particles
+        offset[j] .. offset[j+1]-1 (offset: nexp + 1 device int32 values)."""
+        self._check(self.L.sfmm_p2x_ragged_device(self.h, kind, nexp, _ptr(offset), _ptr(charge), _ptr(pos),
+                                                  _ptr(centre), _ptr(out), out_stride))
 
 
 class Plan:

@@ -646,7 +646,24 @@ int sfmm_p2x_device(sfmm_context *c, int kind, size_t nexp, size_t nq, const dou
     if (!charge || !pos || !centre || !out) return fail(c, SFMM_INVALID_ARG, "null device pointer");
     if (out_stride < (size_t)c->P * (c->P + 1)) return fail(c, SFMM_INVALID_ARG, "stride smaller than P(P+1)");
     cudaSetDevice(c->device);
-    cudaError_t e = launch_p2x(c->dtype == SFMM_F64, kind, c->P, (long long)nexp, (long long)nq, charge, pos, centre,
+    cudaError_t e = launch_p2x(c->dtype == SFMM_F64, kind, c->P, (long long)nexp, (long long)nq, nullptr, charge,
+                               pos, centre, out, (long long)out_stride, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "P2M/P2L kernel");
+    c->launches++;
+    return SFMM_OK;
+}
+
+int sfmm_p2x_ragged_device(sfmm_context *c, int kind, size_t nexp, const uint32_t *offset, const double *charge,
+                           const double *pos, const double *centre, void *out, size_t out_stride)
+{
+    if (!c) return SFMM_INVALID_ARG;
+    Range range("sfmm p2m/p2l");
+    if (kind != 0 && kind != 1) return fail(c, SFMM_INVALID_ARG, "kind must be 0 (P2M) or 1 (P2L)");
+    if (nexp == 0) return SFMM_OK;
+    if (!offset || !charge || !pos || !centre || !out) return fail(c, SFMM_INVALID_ARG, "null device pointer");
+    if (out_stride < (size_t)c->P * (c->P + 1)) return fail(c, SFMM_INVALID_ARG, "stride smaller than P(P+1)");
+    cudaSetDevice(c->device);
+    cudaError_t e = launch_p2x(c->dtype == SFMM_F64, kind, c->P, (long long)nexp, 0, offset, charge, pos, centre,
                                out, (long long)out_stride, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "P2M/P2L kernel");
     c->launches++;

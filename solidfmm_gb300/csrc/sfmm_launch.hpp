@@ -45,8 +45,10 @@ cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, in
 int translate_blocks_per_sm(Arith a, const LaunchShape &s);
 
 // P2M / P2L (sfmm_p2x.cu)
-cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const double *q,
-                       const double *pos, const double *centre, void *out, long long stride, cudaStream_t st);
+// expansion j takes particles [j nq, (j+1) nq), or [offset[j], offset[j+1]) with an offset array
+cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const uint32_t *offset,
+                       const double *q, const double *pos, const double *centre, void *out, long long stride,
+                       cudaStream_t st);
 
 // L2P / M2P evaluation (sfmm_p2x.cu)
 cudaError_t launch_eval(bool f64, int kind, int P, long long npts, const double *pos, const uint32_t *box,

@@ -18,17 +18,22 @@
 
 namespace sfmm {
 
+// Expansion j takes particles [j nq, (j+1) nq), or [offset[j], offset[j+1])
+// when an offset array is given (ragged leaves).
 template <class Out>
-__global__ void k_p2x(int kind, int P, long long nexp, long long nq, const double *__restrict__ q,
-                      const double *__restrict__ pos, const double *__restrict__ centre, Out *out, long long stride)
+__global__ void k_p2x(int kind, int P, long long nexp, long long nq, const uint32_t *__restrict__ offset,
+                      const double *__restrict__ q, const double *__restrict__ pos,
+                      const double *__restrict__ centre, Out *out, long long stride)
 {
     long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (j >= nexp) return;
     Out *o = out + j * stride;
     const double cx = centre[3 * j], cy = centre[3 * j + 1], cz = centre[3 * j + 2];
-    for (long long k = 0; k < nq; ++k) {
-        const double w = q[j * nq + k];
-        const double *pp = pos + 3 * (j * nq + k);
+    const long long k0 = offset ? (long long)offset[j] : j * nq;
+    const long long k1 = offset ? (long long)offset[j + 1] : (j + 1) * nq;
+    for (long long k = k0; k < k1; ++k) {
+        const double w = q[k];
+        const double *pp = pos + 3 * k;
         const double x = pp[0] - cx, y = pp[1] - cy, z = pp[2] - cz;
         const double r2 = x * x + y * y + z * z;
         if (kind == 0) {
@@ -103,17 +108,20 @@ __global__ void k_p2x(int kind, int P, long long nexp, long long nq, const doubl
     }
 }
 
-cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const double *q, const double *pos,
-                       const double *centre, void *out, long long stride, cudaStream_t st)
+cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const uint32_t *offset,
+                       const double *q, const double *pos, const double *centre, void *out, long long stride,
+                       cudaStream_t st)
 {
     if (nexp == 0) return cudaSuccess;
     int tb = 128;
     long long grid = (nexp + tb - 1) / tb;
     clear_stale_error();
     if (f64)
-        k_p2x<double><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, q, pos, centre, (double *)out, stride);
+        k_p2x<double><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, offset, q, pos, centre, (double *)out,
+                                                      stride);
     else
-        k_p2x<float><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, q, pos, centre, (float *)out, stride);
+        k_p2x<float><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, offset, q, pos, centre, (float *)out,
+                                                     stride);
     return cudaGetLastError();
 }
 

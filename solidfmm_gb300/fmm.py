@@ -10,7 +10,11 @@ batch kept on the GPU:
 * level l has 2^l boxes per side, box (i, j, k) has index (i 2^l + j) 2^l + k
   and centre ((i, j, k) + 1/2) 2^-l; expansions of all levels live in one
   array (level offsets ``offset[l]``), multipoles and locals separately;
-* P2M at the leaves (``sfmm_p2x_device``), then one execution plan
+* arbitrary particles in the unit cube are binned into the leaves on the
+  device (``bin_particles``: leaf index, stable sort, counts -> offsets), so
+  leaves hold any number of particles, none included;
+* P2M at the leaves (``sfmm_p2x_device``, or ``sfmm_p2x_ragged_device`` over
+  each leaf's range of the sorted particles), then one execution plan
   (``sfmm_plan_*``) with the stages M2M depth -> 2 (one per level, targets
   repeat), M2L at levels 2..depth (interaction lists: children of the
   parent's neighbours that are not neighbours, at most 189 per box; targets
@@ -181,8 +185,55 @@ class UniformFMM:
         self.ctx.p2x(0, nleaf, nq, charges, positions, self.leaf_centres, self.M[lo:], self.S)
         self.plan.run()
 
+    def run_particles(self, charges, positions):
+        """One pass for arbitrary particles in the unit cube (charges (n,),
+        positions (n, 3)): bin them into the leaves (``bin_particles``), P2M
+        of every leaf over its own particles, then the plan.  Returns the
+        charges and positions sorted by leaf and keeps the binning in
+        ``order`` and ``leaf_offsets``; ``leaf_of_sorted()`` gives each sorted
+        particle's leaf (the box index for L2P)."""
+        order, off = bin_particles(positions, self.depth)
+        self.order, self.leaf_offsets = order, off
+        q = charges[order].contiguous()
+        p = positions[order].contiguous()
+        self._sorted = (q, p)  # alive until the next pass (the kernels run asynchronously)
+        self.M.zero_()
+        self.L.zero_()
+        lo = self.offsets[self.depth]
+        self.ctx.p2x_ragged(0, 8 ** self.depth, off, q, p, self.leaf_centres, self.M[lo:], self.S)
+        self.plan.run()
+        return q, p
+
+    def leaf_of_sorted(self):
+        """Leaf of every particle of the last ``run_particles``, in sorted order (int32)."""
+        import torch
+
+        counts = (self.leaf_offsets[1:] - self.leaf_offsets[:-1]).to(torch.int64)
+        leaves = torch.arange(len(counts), dtype=torch.int32, device=counts.device)
+        return torch.repeat_interleave(leaves, counts)
+
     def leaf_locals(self):
         return self.L[self.offsets[self.depth]:]
+
+
+def bin_particles(positions, depth: int):
+    """Octree build for arbitrary particles in the unit cube: every particle
+    goes to the leaf box (i, j, k) = floor(x 2^depth) (the face x = 1 to the
+    last box), and the particles are ordered by leaf, stably.  Returns
+    (order, offsets): ``positions[order]`` lists leaf 0's particles first and
+    leaf b's are ``order[offsets[b]:offsets[b+1]]`` (int32, 8^depth + 1
+    entries).  Positions outside [0, 1]^3 raise ValueError."""
+    import torch
+
+    n = 2 ** depth
+    if positions.numel() and (bool((positions < 0).any()) or bool((positions > 1).any())):
+        raise ValueError("particles must lie in the unit cube [0, 1]^3")
+    ijk = (positions * n).floor().to(torch.int64).clamp_(0, n - 1)
+    leaf = (ijk[:, 0] * n + ijk[:, 1]) * n + ijk[:, 2]
+    order = torch.argsort(leaf, stable=True)
+    offsets = torch.zeros(n ** 3 + 1, dtype=torch.int64, device=positions.device)
+    offsets[1:] = torch.cumsum(torch.bincount(leaf, minlength=n ** 3), 0)
+    return order, offsets.to(torch.int32)
 
 
 def random_particles(depth: int, per_leaf: int, seed: int, device):

@@ -72,3 +72,34 @@ def test_oracle_lists_agree_and_stage_counts():
     for x in st:
         if x.op != "m2l":
             assert np.allclose(x.shift.numpy(), cen[x.dst_index.numpy()] - cen[x.src_index.numpy()])
+
+
+def test_bin_particles_sorts_stably_by_leaf():
+    """Every particle lands in the leaf floor(x 2^depth) (the face x = 1 in
+    the last box), leaves come in index order, particles of one leaf keep
+    their input order, the offsets count them, and empty leaves are empty
+    ranges; positions outside the unit cube are refused."""
+    depth = 3
+    n = 2 ** depth
+    g = torch.Generator().manual_seed(4)
+    # clustered particles (two blobs) plus points on faces and corners
+    blobs = torch.cat([0.2 + 0.05 * torch.randn(700, 3, generator=g, dtype=torch.float64),
+                       0.7 + 0.1 * torch.randn(300, 3, generator=g, dtype=torch.float64)]).clamp(0, 1)
+    faces = torch.tensor([[1.0, 1.0, 1.0], [0.0, 0.0, 0.0], [0.5, 1.0, 0.125], [0.125, 0.0, 1.0]],
+                         dtype=torch.float64)
+    pos = torch.cat([blobs, faces])
+    order, off = fmm.bin_particles(pos, depth)
+    assert off.dtype == torch.int32 and len(off) == n ** 3 + 1 and int(off[-1]) == len(pos)
+    x = pos.numpy()
+    ijk = np.minimum(np.floor(x * n).astype(np.int64), n - 1)
+    leaf = (ijk[:, 0] * n + ijk[:, 1]) * n + ijk[:, 2]
+    want = np.argsort(leaf, kind="stable")
+    assert np.array_equal(order.numpy(), want)
+    counts = np.bincount(leaf, minlength=n ** 3)
+    assert np.array_equal(np.diff(off.numpy()), counts)
+    assert (counts == 0).sum() > 0  # the clustered set leaves boxes empty
+    assert int(leaf[len(blobs)]) == n ** 3 - 1 and int(leaf[len(blobs) + 1]) == 0
+    with pytest.raises(ValueError):
+        fmm.bin_particles(torch.tensor([[0.5, 0.5, 1.5]], dtype=torch.float64), depth)
+    with pytest.raises(ValueError):
+        fmm.bin_particles(torch.tensor([[-1e-9, 0.5, 0.5]], dtype=torch.float64), depth)

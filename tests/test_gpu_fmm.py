@@ -81,3 +81,74 @@ def test_fmm_potential_against_direct_sum(native, fmm_case):
     err = np.linalg.norm(far + near - direct) / np.linalg.norm(direct)
     assert leaf_of.shape == far.shape
     assert err < 1e-4, err
+
+
+def test_fmm_arbitrary_particles(native, oracle):
+    """Clustered particles in the unit cube (two blobs: leaves hold 0 to
+    about 100 particles) binned on the GPU, P2M over each leaf's own range,
+    one pass: the leaf locals match the oracle's pass over the same leaves
+    (binned here with numpy, each leaf padded with zero charges), and the
+    potential at every particle (far field by L2P at its leaf, near field by
+    direct sums over the neighbour leaves) matches direct summation."""
+    import torch
+    from solidfmm_gb300 import fmm
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fmm_oracle
+
+    depth, P = 3, 10
+    n, nleaf = 2 ** depth, 8 ** depth
+    rng = np.random.default_rng(21)
+    x = np.concatenate([0.25 + 0.06 * rng.standard_normal((1500, 3)), 0.7 + 0.12 * rng.standard_normal((900, 3)),
+                        rng.random((300, 3))])
+    x = np.clip(x, 0.0, 1.0 - 1e-12)
+    qq = rng.uniform(-1, 1, len(x))
+    ijk = np.floor(x * n).astype(np.int64)
+    leaf = (ijk[:, 0] * n + ijk[:, 1]) * n + ijk[:, 2]
+    counts = np.bincount(leaf, minlength=nleaf)
+    assert counts.min() == 0 and counts.max() > 40
+    Q = np.zeros((nleaf, counts.max()))
+    X = np.repeat(((np.stack(np.unravel_index(np.arange(nleaf), (n, n, n)), 1) + 0.5) / n)[:, None, :],
+                  counts.max(), axis=1)
+    fill = np.zeros(nleaf, np.int64)
+    for k in np.argsort(leaf, kind="stable"):
+        b = leaf[k]
+        Q[b, fill[b]] = qq[k]
+        X[b, fill[b]] = x[k]
+        fill[b] += 1
+    ref = fmm_oracle.fmm_pass(depth, P, Q, X)
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    tq, tx = torch.as_tensor(qq, device=dev), torch.as_tensor(x, device=dev)
+    w = norm_weights(P, "L")
+    for prec, tol in ((0, 1e-12), (1, 1e-7)):
+        f = fmm.UniformFMM(ctx, depth, prec, dev)
+        sq, sx = f.run_particles(tq, tx)
+        torch.cuda.synchronize()
+        assert rel_err(f.leaf_locals().cpu().numpy(), ref, w) < tol, prec
+    # potential of the split pass at every particle
+    box = f.leaf_of_sorted()
+    pot = torch.zeros(len(x), dtype=torch.float64, device=dev)
+    ctx.evaluate(0, len(x), sx, f.leaf_locals(), f.S, nleaf, f.leaf_centres, pot, box=box)
+    torch.cuda.synchronize()
+    far = pot.cpu().numpy()
+    xs, qs, lb = sx.cpu().numpy(), sq.cpu().numpy(), box.cpu().numpy().astype(np.int64)
+    off = f.leaf_offsets.cpu().numpy().astype(np.int64)
+    ns, nt = fmm.neighbours(depth)
+    nbr = [[] for _ in range(nleaf)]
+    for a, b in zip(ns.tolist(), nt.tolist()):
+        nbr[b].append(a)
+    near = np.zeros(len(xs))
+    for b in range(nleaf):
+        if off[b] == off[b + 1]:
+            continue
+        src = np.concatenate([np.arange(off[a], off[a + 1]) for a in nbr[b]])
+        tgt = np.arange(off[b], off[b + 1])
+        r = np.linalg.norm(xs[tgt][:, None, :] - xs[src][None, :, :], axis=2)
+        with np.errstate(divide="ignore"):
+            near[tgt] = (np.where(r > 0, 1.0 / r, 0.0) * qs[src][None, :]).sum(1)
+    r = np.linalg.norm(xs[:, None, :] - xs[None, :, :], axis=2)
+    with np.errstate(divide="ignore"):
+        direct = (np.where(r > 0, 1.0 / r, 0.0) * qs[None, :]).sum(1)
+    assert np.array_equal(lb, leaf[f.order.cpu().numpy()])
+    assert np.linalg.norm(far + near - direct) / np.linalg.norm(direct) < 1e-4
