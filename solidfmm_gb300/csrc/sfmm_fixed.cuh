@@ -62,34 +62,26 @@ __device__ __forceinline__ ff fixed_to_ff(int m, int E)
 
 // Shift that brings the int64 accumulators of one degree row (all G threads
 // of the translation) to at most kFixBits bits; the block exponent grows by
-// the shift.  Only the high words are inspected: with h the OR of their
-// one's-complement magnitudes (h ^ (h >> 31) is |h| or |h| - 1), every
-// value satisfies |v| <= 2^(32 + bitlen(h)), so a shift of
-// 32 + bitlen(h) - kFixBits leaves at most kFixBits bits (v = -2^k narrows
-// to exactly -2^kFixBits).  A swap of a normalised row (largest mantissa at
-// least 2^29, orthogonal unit rows, Q1.30 coefficients) leaves its largest
-// value at 2^56 or more, whose bit length the high word gives exactly: the
-// shift is the one the full 64-bit magnitudes would give.  The group maximum
-// runs on the 32-bit bit lengths; the shift is at least 2.
+// the shift.  The bit length comes from the OR of one's-complement
+// magnitudes: v ^ (v >> 63) is |v| or |v| - 1, whose bit length can only
+// undercount for v = -2^k, which then narrows to exactly -2^kFixBits.  The
+// group maximum runs on the 32-bit bit lengths.
 template <int G, int NA>
 __device__ __forceinline__ int group_renorm_shift(const long long (&ar)[NA], const long long (&ai)[NA])
 {
-    unsigned o = 0;
+    unsigned long long o = 0;
 #pragma unroll
-    for (int a = 0; a < NA; ++a) {
-        const int hr = (int)(ar[a] >> 32), hi = (int)(ai[a] >> 32);
-        o |= (unsigned)(hr ^ (hr >> 31)) | (unsigned)(hi ^ (hi >> 31));
-    }
-    int used = 32 - __clz((int)o);
+    for (int a = 0; a < NA; ++a)
+        o |= (unsigned long long)(ar[a] ^ (ar[a] >> 63)) | (unsigned long long)(ai[a] ^ (ai[a] >> 63));
+    int used = 64 - __clzll((long long)o);
 #pragma unroll
     for (int k = 1; k < G; k <<= 1) used = max(used, __shfl_xor_sync(0xffffffffu, used, k));
-    return used + 32 - kFixBits;
+    return used > kFixBits ? used - kFixBits : 0;
 }
 
-// round(a / 2^s) for a shift of at least 1
 __device__ __forceinline__ int round_shift(long long a, int s)
 {
-    return (int)((a + (1ll << (s - 1))) >> s);
+    return s ? (int)((a + (1ll << (s - 1))) >> s) : (int)a;
 }
 
 // (c*x - s*y) in Q1.30, rounded
