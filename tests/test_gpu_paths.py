@@ -406,3 +406,38 @@ def test_device_strides_wider_than_expansions(native, ctx64, oracle, prec):
     w = norm_weights(P, "L")
     tol = {0: 1e-12, 1: 1e-7, 2: 1e-11}[prec]
     assert rel_err(got[:, :S] - b["dst"], ref - b["dst"], w) < tol
+
+
+@pytest.mark.parametrize("op", ["m2m", "m2l", "l2l"])
+def test_fp32_high_orders_vs_fp64_oracle(native, oracle, op):
+    """FP32 contexts at orders 24 and 28 (8 threads per translation, the
+    FP32 limit of this library; the reference's float stops at 18), against
+    the FP64 oracle in the orthonormal basis.  Measured maxima (GB300): M2M
+    3.8e-6 at 24 and 1.2e-5 at 28, M2L 1.6e-6 and L2L 5e-7 at 28."""
+    for P, tol in ((24, 2e-5), (28, 5e-5)):
+        ctx = native.Context(P, "f32")
+        b = _batch(op, P, P, 64, 60 + P)
+        ref = _oracle(oracle, op, b)
+        got = run_device(ctx, op, 0, b["src"].astype(np.float32), b["dst"].astype(np.float32), b["Pin"], b["Pout"],
+                         b["xyz"])
+        w = norm_weights(P, "M" if op == "m2m" else "L")
+        err = rel_err(got.astype(np.float64) - b["dst"], ref - b["dst"], w)
+        assert err < tol, (P, err)
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["plain", "split", "split_ff"])
+def test_results_after_tuning(native, oracle, prec):
+    """sfmm_tune keeps the fastest of the group sizes and tile shapes it
+    measured (some orders choose the smallest full-occupancy tile); the
+    batches that follow at those bounds still match the oracle."""
+    ctx = native.Context(24, "f64")
+    for op in ("m2l", "m2m", "l2l"):
+        for bound in (6, 10, 17, 24):
+            g, rate = ctx.tune(op, prec, n=20000, order_bound=bound)
+            assert g in (4, 8) and rate > 0
+            b = _batch(op, (1, bound), (1, bound), 150, 700 + bound)
+            ref = _oracle(oracle, op, b)
+            got = run_device(ctx, op, prec, b["src"], b["dst"], b["Pin"], b["Pout"], b["xyz"], order_bound=bound)
+            w = norm_weights(bound, "M" if op == "m2m" else "L")
+            tol = {0: 1e-12, 1: 1e-7, 2: 1e-11 if bound <= 16 else 1e-9}[prec]
+            assert rel_err(got - b["dst"], ref - b["dst"], w) < tol, (op, bound, g)
