@@ -441,3 +441,47 @@ def test_results_after_tuning(native, oracle, prec):
             w = norm_weights(bound, "M" if op == "m2m" else "L")
             tol = {0: 1e-12, 1: 1e-7, 2: 1e-11 if bound <= 16 else 1e-9}[prec]
             assert rel_err(got - b["dst"], ref - b["dst"], w) < tol, (op, bound, g)
+
+
+@pytest.mark.parametrize("order", ["ascending", "runs", "shuffled", "descending"])
+def test_classic_host_call_fp32(native, oracle, order):
+    """The pointer-array call on an FP32 context: float solids (rows of one
+    float array) and float shifts, targets in the four orders of the
+    bookkeeping (repeats accumulate in device slots), against the FP64
+    oracle on the same (float-rounded) inputs."""
+    import ctypes as C
+
+    L = native.load()
+    P, S = 12, 156
+    rng = np.random.default_rng({"ascending": 91, "runs": 92, "shuffled": 93, "descending": 94}[order])
+    n = 2000
+    b = _batch("m2l", (1, P), P, n, 95)
+    src = b["src"].astype(np.float32)
+    xyz = b["xyz"].astype(np.float32)
+    pin = b["Pin"].astype(np.int64)
+    if order in ("ascending", "descending"):
+        tidx = np.arange(n) if order == "ascending" else np.arange(n)[::-1].copy()
+        nt = n
+    else:
+        tidx = np.sort(rng.integers(0, 300, size=n))
+        nt = 300
+        if order == "shuffled":
+            rng.shuffle(tidx)
+    dst = (rng.normal(size=(nt, S)) * 1e-3).astype(np.float32)
+    start = dst.astype(np.float64)
+    ctx = native.Context(P, "f32")
+    sp = (C.c_void_p * n)(*[src.ctypes.data + i * S * 4 for i in range(n)])
+    dp = (C.c_void_p * n)(*[dst.ctypes.data + int(tidx[i]) * S * 4 for i in range(n)])
+    cin = (C.c_size_t * n)(*[int(v) for v in pin])
+    cout = (C.c_size_t * n)(*([P] * n))
+    x, y, z = (np.ascontiguousarray(xyz[:, k]) for k in range(3))
+    L.sfmm_translate_host.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_size_t, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p]
+    rc = L.sfmm_translate_host(ctx.h, 1, 0, n, sp, cin, dp, cout, 1, x.ctypes.data, y.ctypes.data, z.ctypes.data)
+    assert rc == 0, L.sfmm_last_error(ctx.h)
+    ref = start.copy()
+    oracle.naive("m2l", src.astype(np.float64), pin.astype(np.uint32), ref, np.full(n, P, np.uint32),
+                 xyz.astype(np.float64), tidx=tidx.astype(np.uint32))
+    got = dst.astype(np.float64)
+    # float targets: the error of summing in FP32 on top of the translation's
+    assert rel_err(got - start, ref - start, norm_weights(P, "L")) < 2e-5
