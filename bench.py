@@ -744,7 +744,9 @@ def main():
             "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the split kernel, "
                                f"{tb:.0f} B per translation on 65 536 translations, scaled to {N}") if tb else None,
             "peak_source": peak_src, "kernel": "k_translate<ff, G, ACC, fixed> (split)",
-            "bytes_per_translation": B}
+            "bytes_per_translation": B,
+            "binding": "instruction issue on the FP32/INT pipes, not HBM (DRAM traffic equals the algorithmic "
+                       "bytes): see roofline_issue"}
     roof_issue = None
     ipt = INSTRUCTIONS.get((op, P))
     if ipt and clk and clk.get("sm_mhz"):
