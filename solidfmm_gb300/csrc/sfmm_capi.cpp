@@ -77,47 +77,6 @@ cudaError_t upload(void **dst, const std::vector<double> &v, Arith a)
     return cudaMemcpy(*dst, bytes.data(), bytes.size(), cudaMemcpyHostToDevice);
 }
 
-int ensure_tables(sfmm_context *c, Arith a)
-{
-    DevTables &t = c->tab[(int)a];
-    if (t.ready) return SFMM_OK;
-    cudaError_t e;
-    const size_t n8 = c->host.woff8.size();
-    if (!c->d_woff) {
-        if ((e = cudaMalloc(&c->d_woff, sizeof(int) * c->P)) != cudaSuccess ||
-            (e = cudaMalloc(&c->d_hoff, sizeof(int) * c->P)) != cudaSuccess ||
-            (e = cudaMemcpy(c->d_woff, c->host.woff.data(), sizeof(int) * c->P, cudaMemcpyHostToDevice)) != cudaSuccess ||
-            (e = cudaMemcpy(c->d_hoff, c->host.hoff.data(), sizeof(int) * c->P, cudaMemcpyHostToDevice)) != cudaSuccess)
-            return cuda_fail(c, e, "table upload");
-        if (n8 && ((e = cudaMalloc(&c->d_woff8, sizeof(int) * n8)) != cudaSuccess ||
-                   (e = cudaMemcpy(c->d_woff8, c->host.woff8.data(), sizeof(int) * n8, cudaMemcpyHostToDevice)) !=
-                       cudaSuccess))
-            return cuda_fail(c, e, "table upload");
-    }
-    if ((e = upload(&t.W, c->host.W, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-    if (n8 && (e = upload(&t.W8, c->host.W8, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-    if ((e = upload(&t.ein_M, c->host.e_in_M, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-    if ((e = upload(&t.ein_L, c->host.e_in_L, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-    if ((e = upload(&t.eout_L, c->host.e_out_L, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-    if ((e = upload(&t.eout_M, c->host.e_out_M, a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-    for (int k = 0; k < 3; ++k)
-        if ((e = upload(&t.H[k], c->host.H[k], a)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-    if (a == Arith::FFQ) {
-        // |w| <= 1 (orthogonal matrices): round(w 2^30) fits int32
-        auto upload_q30 = [](void **dst, const std::vector<double> &W) {
-            std::vector<int32_t> q(W.size());
-            for (size_t i = 0; i < q.size(); ++i) q[i] = (int32_t)std::llround(std::ldexp(W[i], 30));
-            cudaError_t err = cudaMalloc(dst, q.size() * sizeof(int32_t) + 16);
-            if (err == cudaSuccess) err = cudaMemcpy(*dst, q.data(), q.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
-            return err;
-        };
-        if ((e = upload_q30(&t.Wq, c->host.W)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-        if (n8 && (e = upload_q30(&t.Wq8, c->host.W8)) != cudaSuccess) return cuda_fail(c, e, "table upload");
-    }
-    t.ready = true;
-    return SFMM_OK;
-}
-
 void free_tables(DevTables &t)
 {
     void *ps[] = {t.W, t.ein_M, t.ein_L, t.eout_L, t.eout_M, t.H[0], t.H[1], t.H[2], t.Wq, t.W8, t.Wq8};
@@ -125,6 +84,71 @@ void free_tables(DevTables &t)
         if (p) cudaFree(p);
     t = DevTables{};
 }
+
+namespace {
+
+void free_offsets(sfmm_context *c)
+{
+    int **ps[] = {&c->d_woff, &c->d_hoff, &c->d_woff8};
+    for (int **p : ps) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+}
+
+// the offset arrays of the tables, all or none (a partial set is freed)
+cudaError_t upload_offsets(sfmm_context *c)
+{
+    const size_t n8 = c->host.woff8.size();
+    if (c->d_woff && c->d_hoff && (!n8 || c->d_woff8)) return cudaSuccess;
+    free_offsets(c);
+    cudaError_t e = cudaMalloc(&c->d_woff, sizeof(int) * c->P);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_hoff, sizeof(int) * c->P);
+    if (e == cudaSuccess && n8) e = cudaMalloc(&c->d_woff8, sizeof(int) * n8);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(c->d_woff, c->host.woff.data(), sizeof(int) * c->P, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(c->d_hoff, c->host.hoff.data(), sizeof(int) * c->P, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n8)
+        e = cudaMemcpy(c->d_woff8, c->host.woff8.data(), sizeof(int) * n8, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) free_offsets(c);
+    return e;
+}
+
+}  // namespace
+
+int ensure_tables(sfmm_context *c, Arith a)
+{
+    DevTables &t = c->tab[(int)a];
+    if (t.ready) return SFMM_OK;
+    cudaError_t e = upload_offsets(c);
+    if (e != cudaSuccess) return cuda_fail(c, e, "table upload");
+    const bool w8 = !c->host.W8.empty();
+    // |w| <= 1 (orthogonal matrices): round(w 2^30) fits int32
+    auto upload_q30 = [](void **dst, const std::vector<double> &W) {
+        std::vector<int32_t> q(W.size());
+        for (size_t i = 0; i < q.size(); ++i) q[i] = (int32_t)std::llround(std::ldexp(W[i], 30));
+        cudaError_t err = cudaMalloc(dst, q.size() * sizeof(int32_t) + 16);
+        if (err == cudaSuccess) err = cudaMemcpy(*dst, q.data(), q.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+        return err;
+    };
+    e = upload(&t.W, c->host.W, a);
+    if (e == cudaSuccess && w8) e = upload(&t.W8, c->host.W8, a);
+    if (e == cudaSuccess) e = upload(&t.ein_M, c->host.e_in_M, a);
+    if (e == cudaSuccess) e = upload(&t.ein_L, c->host.e_in_L, a);
+    if (e == cudaSuccess) e = upload(&t.eout_L, c->host.e_out_L, a);
+    if (e == cudaSuccess) e = upload(&t.eout_M, c->host.e_out_M, a);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = upload(&t.H[k], c->host.H[k], a);
+    if (e == cudaSuccess && a == Arith::FFQ) e = upload_q30(&t.Wq, c->host.W);
+    if (e == cudaSuccess && a == Arith::FFQ && w8) e = upload_q30(&t.Wq8, c->host.W8);
+    if (e != cudaSuccess) {
+        free_tables(t);  // a partial set is retried from scratch on the next call
+        return cuda_fail(c, e, "table upload");
+    }
+    t.ready = true;
+    return SFMM_OK;
+}
+
 
 int arith_of(sfmm_context *c, int precision, Arith *out)
 {
@@ -399,6 +423,7 @@ int sfmm_create(sfmm_context **out, int dtype, size_t P, int device)
         return SFMM_OOM;
     }
     if (cudaMalloc(&c->d_status, sizeof(int)) != cudaSuccess || cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess) {
+        if (c->d_status) cudaFree(c->d_status);
         delete c;
         return SFMM_CUDA_ERROR;
     }
@@ -420,9 +445,7 @@ void sfmm_destroy(sfmm_context *c)
     }
     c->d_work.release();
     if (c->d_status) cudaFree(c->d_status);
-    if (c->d_woff) cudaFree(c->d_woff);
-    if (c->d_woff8) cudaFree(c->d_woff8);
-    if (c->d_hoff) cudaFree(c->d_hoff);
+    free_offsets(c);
     c->h_src.release();
     c->h_dst.release();
     c->h_meta.release();

@@ -205,6 +205,13 @@ int sfmm_plan_finalize(sfmm_plan *p)
     sfmm_context *c = p->ctx;
     if (p->finalized) return fail(c, SFMM_INVALID_ARG, "plan already finalized");
     if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, SFMM_CUDA_ERROR, "cannot select device %d", c->device);
+    // a failed finalize may be retried (after fixing the stage data): start clean
+    p->launches = 0;
+    for (Stage &s : p->stages) s.segs.clear();
+    if (p->d_perm) {
+        cudaFree(p->d_perm);
+        p->d_perm = nullptr;
+    }
     // 1. sort every stage by (bound, p_in, p_out) on the host
     std::vector<uint32_t> perm;
     try {

@@ -148,3 +148,32 @@ def test_plan_errors(native):
         plan.add("m2l", 0, 4, src, S, 4, dst, S, 4, ok, ok, sh)
     with pytest.raises(native.SfmmError, match="INVALID_ARG"):
         native.Plan(ctx).add("m2l", 0, 4, src, 20, 4, dst, S, 4, ok, ok, sh).finalize()
+
+
+def test_plan_finalize_retried_after_fixing_orders(native, oracle):
+    """A finalize that fails on an order above the context's leaves the plan
+    unfinalized; after the stage's orders are corrected on the device, a
+    second finalize records each translation once and the replay matches the
+    oracle."""
+    import torch
+
+    P = 10
+    ctx = native.Context(P, "f64")
+    b = _batch("m2l", (1, P), (1, P), 200, 51)
+    t = _dev(b)
+    S = b["src"].shape[1]
+    n = len(b["Pin"])
+    good = t["Pin"].clone()
+    t["Pin"][7] = P + 3
+    d = t["dst"].clone()
+    plan = native.Plan(ctx)
+    plan.add("m2l", 0, n, t["src"], S, n, d, S, n, t["Pin"], t["Pout"], t["xyz"])
+    with pytest.raises(native.SfmmError, match="ORDER_RANGE"):
+        plan.finalize()
+    t["Pin"].copy_(good)
+    plan.finalize()
+    assert sum(s[1] for s in plan.segments()) == n
+    plan.run()
+    torch.cuda.synchronize()
+    ref = _oracle(oracle, "m2l", b)
+    assert rel_err(d.cpu().numpy() - b["dst"], ref - b["dst"], norm_weights(P, "L")) < 1e-12
