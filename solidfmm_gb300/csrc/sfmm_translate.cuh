@@ -31,6 +31,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "sfmm_arith.cuh"
 #include "sfmm_fixed.cuh"
@@ -110,6 +111,10 @@ __device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ W, 
 {
     using T = typename AR::T;
     constexpr int R = swap_rows<G, NA>();
+    // unrolling measured on GB300 (M2L P=16): FP64 runs best rolled (its
+    // pipe is the limit; +3% against 2), float-float unrolled twice (-10%
+    // rolled)
+    constexpr int kUnroll = std::is_same<T, double>::value ? 1 : 2;
     const int jr0 = (q + n) & 1, ji0 = jr0 ^ 1;
     const int cnt = (d + 1) >> 1;  // iterations of the longer part
     const T *w = W + q;
@@ -122,7 +127,7 @@ __device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ W, 
         wrn[a] = AR::ldt(w + G * a);
         win[a] = AR::ldt(w + R + G * a);
     }
-#pragma unroll 2
+#pragma unroll kUnroll
     for (int t = 0; t < cnt; ++t) {
         const T xr = xrn, xi = xin;
         T wr[NA], wi[NA];
@@ -571,7 +576,6 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
     const int q = tid % G;
     const int slot = tid / G;
     const int P = p.P;
-    const int Scap = P * (P + 1);
     const unsigned FULL = 0xffffffffu;
 
     S *buf0 = reinterpret_cast<S *>(smem);
