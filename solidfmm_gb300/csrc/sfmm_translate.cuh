@@ -87,12 +87,11 @@ __device__ __forceinline__ void dispatch(int na, F &&f)
 // for orders up to 32 (G = 4 or 8) and of 32 above (G = 32), so the row
 // count of every degree served by one (G, NA) instance is the same
 // compile-time constant.
-// The two swap passes of a degree: unrolled for FP64 (the FP64 pipe is the
-// limit and the second pass's loads overlap the first's tail: +1.5-2% at
-// P=16 on GB300), rolled for the FP32-pipe arithmetics (-1% split, -5%
-// float-float unrolled)
+// The two swap passes of a degree: unrolled for FP64 and FP32 (the second
+// pass's loads overlap the first's tail: +1.8% FP64, +3% FP32 at P=20 on
+// GB300), rolled for float-float (-5% unrolled)
 template <class T>
-constexpr int kPassUnroll = std::is_same<T, double>::value ? 2 : 1;
+constexpr int kPassUnroll = std::is_same<T, double>::value || std::is_same<T, float>::value ? 2 : 1;
 
 template <int G, int NA>
 __host__ __device__ constexpr int swap_rows()
@@ -118,10 +117,10 @@ __device__ __forceinline__ void swap_both(const typename AR::T *__restrict__ W, 
 {
     using T = typename AR::T;
     constexpr int R = swap_rows<G, NA>();
-    // unrolling measured on GB300 (M2L P=16): FP64 runs best rolled (its
-    // pipe is the limit; +3% against 2), float-float unrolled twice (-10%
-    // rolled)
-    constexpr int kUnroll = std::is_same<T, double>::value ? 1 : 2;
+    // unrolling measured on GB300: FP64 runs best rolled (its pipe is the
+    // limit; +3% at M2L P=16), FP32 unrolled four times (+7% at P=16 with the
+    // passes unrolled too), float-float twice (-10% rolled)
+    constexpr int kUnroll = std::is_same<T, double>::value ? 1 : (std::is_same<T, float>::value ? 4 : 2);
     const int jr0 = (q + n) & 1, ji0 = jr0 ^ 1;
     const int cnt = (d + 1) >> 1;  // iterations of the longer part
     const T *w = W + q;
