@@ -328,21 +328,30 @@ int default_group(Arith a, int P)
 // and registers permitting) for G threads per translation; ties go to the
 // larger tile (fewer CTAs), or to the smaller one with small_tiles (shorter
 // waits at the tile barriers).
-LaunchShape best_shape(Arith a, int P, int G, bool small_tiles)
+LaunchShape best_shape(Arith a, int P, int G, bool small_tiles, int min_threads)
 {
-    LaunchShape best;
-    long best_threads = 0;
-    for (int ts = 256 / G; ts >= 32 / G; ts -= 32 / G) {
-        LaunchShape s = translate_shape(a, P, G, ts);
-        if (!s.acc) continue;
-        s.blocks_per_sm = translate_blocks_per_sm(a, s);
-        long th = (long)s.blocks_per_sm * s.threads;
-        if (th > best_threads || (small_tiles && th == best_threads)) {
-            best_threads = th;
-            best = s;
+    // By default CTAs of at least four warps: one-warp tiles can hold a few
+    // more threads per SM at high orders, but ran up to 40% slower on GB300
+    // (split M2L P=22: 1 976 CTAs of 32 threads, instruction-fetch stalls and
+    // a lower L1 hit rate for the tables); smaller CTAs when no larger tile
+    // fits, or when sfmm_tune measures them faster (split P=27: +6%).
+    for (int floor_threads : {min_threads, 32}) {
+        LaunchShape best;
+        long best_threads = 0;
+        for (int ts = 256 / G; ts >= 32 / G; ts -= 32 / G) {
+            if (G * ts < floor_threads) break;
+            LaunchShape s = translate_shape(a, P, G, ts);
+            if (!s.acc) continue;
+            s.blocks_per_sm = translate_blocks_per_sm(a, s);
+            long th = (long)s.blocks_per_sm * s.threads;
+            if (th > best_threads || (small_tiles && th == best_threads)) {
+                best_threads = th;
+                best = s;
+            }
         }
+        if (best.acc) return best;
     }
-    return best;
+    return LaunchShape{};
 }
 
 cudaError_t launch_translate_64(const KParams &, const LaunchShape &, int, cudaStream_t);
@@ -567,12 +576,21 @@ int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t
     const auto key = std::make_pair((int)a, Pb);
     LaunchShape best;
     double best_rate = 0;
-    const int groups[] = {4, 8, 32};
-    for (int cand = 0; cand < 6; ++cand) {
-        const int G = groups[cand / 2];
-        LaunchShape s = best_shape(a, Pb, G, cand & 1);
-        if (!s.acc) continue;
-        if ((cand & 1) && s.TS == best_shape(a, Pb, G, false).TS) continue;  // the same shape twice
+    // candidates: every group size that runs at this order, each with the
+    // largest and the smallest full-occupancy tile, among CTAs of four warps
+    // or more and among all tiles (distinct shapes only)
+    LaunchShape cands[12];
+    int ncand = 0;
+    for (int G : {4, 8, 32})
+        for (int min_threads : {128, 32})
+            for (bool small : {false, true}) {
+                const LaunchShape s = best_shape(a, Pb, G, small, min_threads);
+                bool seen = !s.acc;
+                for (int k = 0; k < ncand && !seen; ++k) seen = cands[k].G == s.G && cands[k].TS == s.TS;
+                if (!seen) cands[ncand++] = s;
+            }
+    for (int ci = 0; ci < ncand; ++ci) {
+        const LaunchShape s = cands[ci];
         set_shape(c, key, &s);
         float ms = 0;
         for (int rep = 0; rep < 2 && st == SFMM_OK; ++rep) {  // warm-up, then timed

@@ -38,7 +38,10 @@ struct LaunchShape {
 
 LaunchShape translate_shape(Arith a, int P, int G, int ts);
 int default_group(Arith a, int P);
-LaunchShape best_shape(Arith a, int P, int G, bool small_tiles = false);
+// the tile with the most resident threads per SM for G threads per
+// translation (ties: the larger tile, or the smaller with small_tiles), among
+// CTAs of at least min_threads threads when one fits
+LaunchShape best_shape(Arith a, int P, int G, bool small_tiles = false, int min_threads = 128);
 
 // Launch the fused translation kernel (defined in sfmm_k{64,32,ff,ffq}.cu).
 cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, int grid, cudaStream_t st);
