@@ -311,13 +311,13 @@ LaunchShape translate_shape(Arith a, int P, int G, int ts)
 // 8 from a sweep on GB300 (M2L, uniform orders 2..32, both group sizes): 8
 // threads pay off once the per-translation buffers limit the SM to a few
 // warps and the group's own arithmetic is cheap enough to leave latency
-// exposed (FP64 from order 24, FP32 from 24, both split modes from 14).
+// exposed (FP64 from order 24, FP32 from 17, both split modes from 14).
 int default_group(Arith a, int P)
 {
     if (P > 32) return 32;
     switch (a) {
     case Arith::F64: return P >= 24 ? 8 : 4;
-    case Arith::F32: return P >= 24 ? 8 : 4;
+    case Arith::F32: return P >= 17 ? 8 : 4;
     case Arith::FF: return P >= 14 ? 8 : 4;
     case Arith::FFQ: return P >= 14 ? 8 : 4;
     }
