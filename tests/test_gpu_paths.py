@@ -485,3 +485,34 @@ def test_classic_host_call_fp32(native, oracle, order):
     got = dst.astype(np.float64)
     # float targets: the error of summing in FP32 on top of the translation's
     assert rel_err(got - start, ref - start, norm_weights(P, "L")) < 2e-5
+
+
+@pytest.mark.parametrize("memory", ["pinned", "pageable"])
+def test_host_packed_fp32(native, oracle, memory):
+    """The packed host call on an FP32 context (4-byte expansions): distinct
+    targets in place over the host link, repeated targets through index
+    arrays on the staged path, both against the FP64 oracle on the same
+    float-rounded inputs."""
+    import torch
+
+    P = 12
+    ctx = native.Context(P, "f32")
+    d = _batch("m2l", (1, P), (1, P), 500, 63)
+    r = _batch("m2l", (1, P), (1, P), 500, 64, pattern="repeat")
+    for b, repeat in ((d, False), (r, True)):
+        src32 = b["src"].astype(np.float32)
+        dst32 = b["dst"].astype(np.float32)
+        if memory == "pinned":
+            src = torch.from_numpy(src32).pin_memory().numpy()
+            dst = torch.from_numpy(dst32).pin_memory().numpy()
+        else:
+            src, dst = src32.copy(), dst32.copy()
+        start = dst.astype(np.float64)
+        ref = start.copy()
+        oracle.naive("m2l", src32.astype(np.float64), b["Pin"], ref, b["Pout"], b["xyz"], sidx=b["sidx"],
+                     tidx=b["tidx"])
+        ctx.translate_host_packed("m2l", 0, src, dst, b["Pin"], b["Pout"], b["xyz"],
+                                  src_index=b["sidx"] if repeat else None, dst_index=b["tidx"] if repeat else None,
+                                  repeat=repeat)
+        err = rel_err(dst.astype(np.float64) - start, ref - start, norm_weights(P, "L"))
+        assert err < 2e-5, (repeat, err)
