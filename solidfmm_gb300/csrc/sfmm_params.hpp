@@ -26,6 +26,7 @@ struct KParams {
     const uint32_t *perm;
     long long nidx;     // entries of pin/pout/shift/sidx/tidx (perm values index these)
     int atomic;
+    int prefetch;  // L2 prefetch of targets and next sources (device memory; off for host memory)
     const void *W;      // arith-typed swap matrices (padded, see sfmm_tables.hpp)
     const int *Wq;      // swap matrices in Q1.30 (fixed-point variant), same layout as W
     const int *woff;    // offset of degree n's W blocks

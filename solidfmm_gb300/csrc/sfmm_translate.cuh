@@ -668,9 +668,10 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
 
         // L2 prefetch, spread over the group: this tile's targets (read at the
         // end of the tile) and the next tile's sources (read at its start),
-        // so that both phases meet L2 instead of DRAM.  Device arrays only;
-        // every address lies inside an expansion the entry may touch.
-        if (!p.src_ptr) {
+        // so that both phases meet L2 instead of DRAM.  Device arrays only
+        // (host memory read over the link is better left to the demand
+        // loads); every address lies inside an expansion the entry may touch.
+        if (p.prefetch && !p.src_ptr) {
             const int tc = max(pout * (pout + 1), ident_p * (ident_p + 1));
             if (valid && tc) {
                 const char *dp = reinterpret_cast<const char *>(dst + (long long)ti * p.dstride);
