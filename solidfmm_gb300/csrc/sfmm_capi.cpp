@@ -220,7 +220,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
               long long sstride, long long nsrc, const uint32_t *sidx, void *dst, long long dstride, long long ndst,
               const uint32_t *tidx, const uint32_t *pin, const uint32_t *pout, const double *shift,
               const uint32_t *perm, int flags, long long nidx, const unsigned long long *src_ptr,
-              const unsigned long long *dst_ptr, bool prefetch)
+              const unsigned long long *dst_ptr, bool in_hbm)
 {
     if (n == 0) return SFMM_OK;
     static const char *const kName[3] = {"sfmm m2m launch", "sfmm m2l launch", "sfmm l2l launch"};
@@ -253,7 +253,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.src_ptr = src_ptr;
     p.dst_ptr = dst_ptr;
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
-    p.prefetch = prefetch ? 1 : 0;
+    p.in_hbm = in_hbm ? 1 : 0;
     // swap blocks padded for this launch's group size (4 or 8 threads per
     // translation step 8 rows, one warp 32)
     const bool w8 = s.G != 32 && c->d_woff8;
@@ -788,8 +788,8 @@ int sfmm_translate_host_packed(sfmm_context *c, int op, int precision, size_t n,
                 (e = cudaMemcpyAsync(dm + n, p_out, n * 4, cudaMemcpyHostToDevice, s)) ||
                 (e = cudaMemcpyAsync(dsh, shift, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s)))
                 return cuda_fail(c, e, "host-to-device copy");
-            // no L2 prefetch: over the host link it competes with the demand
-            // reads (e2e 43.7 vs 42.3 M translations/s at P=16 without it)
+            // the host-memory instance: no L2 prefetch, no unrolled gather
+            // (over the link both compete with the demand reads)
             st = run_batch(c, s, op, a, (int)pmax, (long long)n, vs, (long long)src_stride, (long long)src_count,
                            nullptr, vd, (long long)dst_stride, (long long)dst_count, nullptr, dm, dm + n, dsh, nullptr,
                            flags, -1, nullptr, nullptr, false);
@@ -937,7 +937,7 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
         if (!repeat) {
             st = run_batch(c, s, op, a, (int)pmax, (long long)M, nullptr, 0, (long long)M, nullptr, nullptr, 0,
                            (long long)M, nullptr, d_pin, d_pout, d_sh, nullptr, SFMM_TARGETS_UNIQUE, -1, d_sptr,
-                           d_dptr);
+                           d_dptr, false);
             if (st) return st;
         } else {
             // repeated targets: sums per target in device slots (atomics),
@@ -949,7 +949,7 @@ int sfmm_translate_host(sfmm_context *c, int op, int precision, size_t n, const 
                 return cuda_fail(c, e, "device buffers");
             st = run_batch(c, s, op, a, (int)pmax, (long long)M, nullptr, 0, (long long)M, nullptr, c->d_dst[0].p,
                            (long long)stride, (long long)nt, d_tidx, d_pin, d_pout, d_sh, nullptr, SFMM_TARGETS_REPEAT,
-                           -1, d_sptr, nullptr);
+                           -1, d_sptr, nullptr, false);
             if (st) return st;
             if ((e = launch_add_slots(c->dtype == SFMM_F64, (long long)nt, d_tptr, d_tcnt, c->d_dst[0].p,
                                       (long long)stride, s)) != cudaSuccess)

@@ -129,6 +129,6 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
               const uint32_t *tidx, const uint32_t *pin, const uint32_t *pout, const double *shift,
               const uint32_t *perm, int flags, long long nidx = -1,
               const unsigned long long *src_ptr = nullptr, const unsigned long long *dst_ptr = nullptr,
-              bool prefetch = true);
+              bool in_hbm = true);
 
 }  // namespace sfmm

@@ -12,21 +12,29 @@
 namespace sfmm {
 
 // Launch shapes come from best_shape, whose occupancy query (below) has set
-// the kernel's shared-memory limit on the current device, so a launch (also
-// inside a CUDA graph capture) makes no other runtime call.
+// the kernels' shared-memory limit on the current device, so a launch (also
+// inside a CUDA graph capture) makes no other runtime call.  Each shape has
+// two instances: expansions in device memory, or in host memory read over
+// the link (p.in_hbm).
 template <class A, int G, int ACC, bool FIX>
 static cudaError_t launch_inst(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
     clear_stale_error();
-    k_translate<A, G, ACC, FIX><<<grid, s.threads, s.smem, st>>>(p);
+    if (p.in_hbm)
+        k_translate<A, G, ACC, FIX, true><<<grid, s.threads, s.smem, st>>>(p);
+    else
+        k_translate<A, G, ACC, FIX, false><<<grid, s.threads, s.smem, st>>>(p);
     return cudaGetLastError();
 }
 
+// resident CTAs per SM of the device-memory instance (the shape's grid
+// sizing); the host-memory instance uses no more resources
 template <class A, int G, int ACC, bool FIX>
 static int occupancy_inst(const LaunchShape &s)
 {
-    auto kern = k_translate<A, G, ACC, FIX>;
+    auto kern = k_translate<A, G, ACC, FIX, true>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
+    cudaFuncSetAttribute(k_translate<A, G, ACC, FIX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, s.threads, s.smem) != cudaSuccess) return 0;
     return nb;

@@ -26,7 +26,7 @@ struct KParams {
     const uint32_t *perm;
     long long nidx;     // entries of pin/pout/shift/sidx/tidx (perm values index these)
     int atomic;
-    int prefetch;  // L2 prefetch of targets and next sources (device memory; off for host memory)
+    int in_hbm;    // expansions in device memory (0: host memory read over the link)
     const void *W;      // arith-typed swap matrices (padded, see sfmm_tables.hpp)
     const int *Wq;      // swap matrices in Q1.30 (fixed-point variant), same layout as W
     const int *woff;    // offset of degree n's W blocks

@@ -562,7 +562,9 @@ struct Geometry {
 };
 
 // FIX selects block fixed-point swaps and beta rotations (float-float only).
-template <class A, int G, int ACC, bool FIX = false>
+// HBM: expansions in device memory (L2 prefetch and a 4x unrolled gather);
+// false for host memory read over the link, where both cost end-to-end rate.
+template <class A, int G, int ACC, bool FIX = false, bool HBM = true>
 __global__ void __launch_bounds__(256) k_translate(KParams p)
 {
     using AR = arith<A>;
@@ -662,16 +664,22 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             const Src *sp = p.src_ptr ? reinterpret_cast<const Src *>(p.src_ptr[m_sidx[s]])
                                       : src + (long long)m_sidx[s] * p.sstride;
             S *bp = buf0 + (long long)s * p.spad;
-            for (int c = lane; c < p.spad; c += 32) AR::st(bp + c, c < cnt ? AR::from_src(__ldcs(sp + c)) : AR::zero());
+            if constexpr (HBM) {  // four loads in flight per lane
+#pragma unroll 4
+                for (int c = lane; c < p.spad; c += 32)
+                    AR::st(bp + c, c < cnt ? AR::from_src(__ldcs(sp + c)) : AR::zero());
+            } else {
+                for (int c = lane; c < p.spad; c += 32)
+                    AR::st(bp + c, c < cnt ? AR::from_src(__ldcs(sp + c)) : AR::zero());
+            }
         }
         __syncthreads();
 
         // L2 prefetch, spread over the group: this tile's targets (read at the
         // end of the tile) and the next tile's sources (read at its start),
-        // so that both phases meet L2 instead of DRAM.  Device arrays only
-        // (host memory read over the link is better left to the demand
-        // loads); every address lies inside an expansion the entry may touch.
-        if (p.prefetch && !p.src_ptr) {
+        // so that both phases meet L2 instead of DRAM.  Device arrays only;
+        // every address lies inside an expansion the entry may touch.
+        if (HBM && !p.src_ptr) {
             const int tc = max(pout * (pout + 1), ident_p * (ident_p + 1));
             if (valid && tc) {
                 const char *dp = reinterpret_cast<const char *>(dst + (long long)ti * p.dstride);
