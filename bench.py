@@ -57,12 +57,12 @@ METRIC = "M2L translations/s at P=16, chosen vs plain FP64 GPU at equal rel. err
 # HBM traffic per translation of the split kernel from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum over the launch / 65 536
 # translations, workload m2l16_small); see profiles/
-TRAFFIC = {("m2l", 16): 5634.0}
+TRAFFIC = {("m2l", 16): 5638.0}
 # warp instructions per translation of the split kernel from the same capture
 # (smsp__inst_executed.sum / 65 536): the kernel is issue bound, so its
 # instruction rate against one warp instruction per cycle per SM sub-partition
 # is the roofline that bounds it
-INSTRUCTIONS = {("m2l", 16): 8165.0}
+INSTRUCTIONS = {("m2l", 16): 8131.0}
 
 
 def useful_flops(op, P):
@@ -743,7 +743,7 @@ def main():
             "frac": achieved_gbs / hbm_peak, "traffic": tb * N if tb else None,
             "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the split kernel, "
                                f"{tb:.0f} B per translation on 65 536 translations, scaled to {N}") if tb else None,
-            "peak_source": peak_src, "kernel": "k_translate<ff, G, ACC, fixed> (split)",
+            "peak_source": peak_src, "kernel": "k_translate<ff, G, ACC, fixed, in HBM> (split)",
             "bytes_per_translation": B,
             "binding": "instruction issue on the FP32/INT pipes, not HBM (DRAM traffic equals the algorithmic "
                        "bytes): see roofline_issue"}
