@@ -188,7 +188,9 @@ void sfmm_plan_destroy(sfmm_plan *plan);
 
 /* Bucket a device batch by (p_in, p_out): writes a permutation of 0..n-1 into
  * `order` (device, n entries) so that translations of equal order pairs are
- * contiguous.  Uses ctx scratch; asynchronous. */
+ * contiguous.  Orders above the context order are counted with the context
+ * order (no error: the translation kernels flag such entries).  n above
+ * 2^32 - 1 -> SFMM_INVALID_ARG.  Uses ctx scratch; asynchronous. */
 int sfmm_bucket_by_order(sfmm_context *ctx, size_t n, const uint32_t *p_in, const uint32_t *p_out,
                          uint32_t *order);
 
@@ -200,13 +202,18 @@ int sfmm_bucket_by_order(sfmm_context *ctx, size_t n, const uint32_t *p_in, cons
  * Same result as sfmm_bucket_by_order (a permutation of 0..n-1 in `order`
  * grouping equal (p_in, p_out) pairs; order within a group is unspecified)
  * for orders up to max_order <= 86; larger max_order returns
- * SFMM_ORDER_RANGE and does nothing.  Runs on the CUDA device current at the
- * call and on `stream` (cudaStream_t as void*, NULL = default stream),
+ * SFMM_ORDER_RANGE and does nothing.  p_in/p_out values above max_order are
+ * counted as max_order (no error), so a max_order below the batch's largest
+ * order merges those pairs into the top buckets.  Runs in the CUDA context
+ * current at the call (the current device's primary context if none is) and
+ * on `stream` (cudaStream_t as void*, NULL = default stream),
  * asynchronously.  Its counters live in one fixed 30 KiB device array per
  * GPU that every call shares: concurrent calls whose kernels overlap on the
- * GPU race and must be serialised (e.g. on one stream).  The first call on a
- * device looks up the array's device address, so make it before any stream
- * capture.  Calls no cudaMalloc/cudaFree. */
+ * GPU race and must be serialised (e.g. on one stream).  The array's device
+ * address is looked up on every call outside a stream capture and kept per
+ * context; a call inside a capture uses the address kept for its context,
+ * so make one call in that context before capturing (else
+ * SFMM_INVALID_ARG).  Calls no cudaMalloc/cudaFree. */
 int sfmm_bucket_by_order_noalloc(size_t n, const uint32_t *p_in, const uint32_t *p_out, uint32_t *order,
                                  size_t max_order, void *stream);
 

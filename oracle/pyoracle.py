@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 import subprocess
 
 import numpy as np
@@ -22,7 +23,11 @@ LIB = os.path.join(HERE, "_build", "liboracle.so")
 # for timing (its AVX-512F double kernel mishandles lanes 12-15 of a batch).
 REF_LIB = os.path.join(HERE, "_ref", "libsolidfmm_ref_generic.so")
 REF_LIB_NATIVE = os.path.join(HERE, "_ref", "libsolidfmm_ref.so")
-REF_SRC = "/root/reference"
+# The reference's sources: the copy `make -C oracle stage` leaves under
+# _ref/src (on a machine without a reference checkout), else SFMM_REF_SRC.
+STAGED_SRC = os.path.join(HERE, "_ref", "src")
+REF_SRC = (STAGED_SRC if os.path.isdir(os.path.join(STAGED_SRC, "solidfmm"))
+           else os.environ.get("SFMM_REF_SRC", "/root/reference"))
 
 OPS = {"m2m": 0, "m2l": 1, "l2l": 2}
 
@@ -32,12 +37,25 @@ _f32p = np.ctypeslib.ndpointer(np.float32, flags="C")
 
 
 def build(with_ref: bool | None = None) -> None:
-    """Compile the oracle (and the reference checker when its sources exist)."""
+    """Compile the oracle (and the reference library when its sources exist:
+    both dispatch builds on x86-64, where the generic one is the golden
+    generator, only the native build elsewhere)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if with_ref is None:
         with_ref = os.path.isdir(os.path.join(REF_SRC, "solidfmm"))
     if with_ref:
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+        if REF_SRC != STAGED_SRC:  # keep a copy that travels to machines without the checkout
+            subprocess.run(["make", "-s", "-C", HERE, "stage", f"REF={REF_SRC}"], check=True)
+        target = "ref" if platform.machine() in ("x86_64", "AMD64") else "ref-native"
+        jobs = str(min(16, os.cpu_count() or 1))
+        subprocess.run(["make", "-s", f"-j{jobs}", "-C", HERE, target, f"REF={REF_SRC}"], check=True)
+
+
+def stage_reference() -> str:
+    """Copy the reference's library sources to _ref/src so that they travel to
+    a machine without a reference checkout (git-ignored, never committed)."""
+    subprocess.run(["make", "-s", "-C", HERE, "stage", f"REF={REF_SRC}"], check=True)
+    return STAGED_SRC
 
 
 _lib = None
@@ -67,8 +85,8 @@ def lib():
     return _lib
 
 
-def ref_available() -> bool:
-    return os.path.exists(REF_LIB)
+def ref_available(native: bool = False) -> bool:
+    return os.path.exists(REF_LIB_NATIVE if native else REF_LIB)
 
 
 def ref(native=False):
@@ -86,6 +104,10 @@ def ref(native=False):
         L.ref_dot_d.argtypes = [C.c_size_t, C.c_size_t, _f64p, C.c_size_t, C.c_size_t, _f64p, _f64p]
         L.ref_hw_threads.restype = C.c_uint
         L.ref_bounding_sphere_d.argtypes = [C.c_size_t, _f64p, _f64p, _f64p, C.c_void_p, _f64p]
+        L.ref_mt_batch_create_d.argtypes = [C.c_int, C.c_size_t, C.c_size_t, _f64p]
+        L.ref_mt_batch_create_d.restype = C.c_void_p
+        L.ref_mt_batch_run_d.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.ref_mt_batch_destroy_d.argtypes = [C.c_void_p]
         _ref[path] = L
     return _ref[path]
 
@@ -173,3 +195,29 @@ def p2m(P, charges, pos, centres, singular=False):
 
 def dot(A, PA, B, PB):
     return lib().orc_dot_d(PA, np.ascontiguousarray(A, np.float64), PB, np.ascontiguousarray(B, np.float64))
+
+
+class MtBatch:
+    """n translations between separately allocated solids of order P, timed
+    through the reference's multithreaded_translator<double>::*_unchecked
+    (its own SIMD kernels, one worker per core), set up once."""
+
+    def __init__(self, op, P, xyz, native=True):
+        self.R = ref(native)
+        xyz = np.ascontiguousarray(xyz, np.float64)
+        self.h = self.R.ref_mt_batch_create_d(OPS.get(op, op), P, len(xyz), xyz.reshape(-1))
+        if not self.h:
+            raise RefError(9, self.R.ref_last_error().decode())
+
+    def run(self) -> float:
+        sec = C.c_double(0)
+        assert self.R.ref_mt_batch_run_d(self.h, C.byref(sec)) == 0
+        return sec.value
+
+    def close(self):
+        if self.h:
+            self.R.ref_mt_batch_destroy_d(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -157,9 +157,69 @@ void dotp(size_t PA, size_t dimA, const real *A, size_t PB, size_t dimB, const r
     dot(a, b, res);
 }
 
+// A batch of n translations of one operator between separately allocated
+// solids of order P, set up once and translated many times through
+// multithreaded_translator<double>::*_unchecked, the pattern of the
+// reference's tests/benchmark_multithreaded_translator.cpp:64-88.
+struct MtBatch {
+    int op = 1;
+    size_t P = 0;
+    std::vector<solid<double>> M, L;
+    std::vector<translation_info<double>> items;
+};
+
 } // namespace
 
 extern "C" {
+
+// Sources hold a fixed pseudo-random pattern of magnitude 1e-3 (the cost of
+// the translation does not depend on the values); targets start at zero.
+// Returns nullptr on failure (message in ref_last_error()).
+void *ref_mt_batch_create_d(int op, size_t P, size_t n, const double *xyz)
+{
+    try {
+        auto b = std::make_unique<MtBatch>();
+        b->op = op;
+        b->P = P;
+        solid<double> blank(P);
+        b->M.assign(n, blank);
+        b->L.assign(n, blank);
+        b->items.resize(n);
+        const size_t S = P * (P + 1);
+        uint64_t st = 0x9e3779b97f4a7c15ull;
+        for (size_t i = 0; i < n; ++i) {
+            double *m = b->M[i].memptr();
+            for (size_t c = 0; c < S; ++c) {
+                st = st * 6364136223846793005ull + 1442695040888963407ull;
+                m[c] = 1e-3 * ((double)(st >> 11) * 0x1.0p-53 - 0.5);
+            }
+            b->items[i] = translation_info<double>{&b->M[i], &b->L[i], xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+        }
+        translator<double>(P).m2l(b->items.data(), b->items.data() + std::min<size_t>(n, 1024));  // warm up
+        return b.release();
+    } catch (const std::exception &e) {
+        std::snprintf(g_err, sizeof g_err, "%s", e.what());
+        return nullptr;
+    }
+}
+
+// one unchecked pass over the whole batch; *seconds = its wall time
+int ref_mt_batch_run_d(void *h, double *seconds)
+{
+    auto *b = static_cast<MtBatch *>(h);
+    if (!b) return 1;
+    multithreaded_translator<double> &tr = translator<double>(b->P);
+    auto *first = b->items.data(), *last = b->items.data() + b->items.size();
+    auto t0 = std::chrono::steady_clock::now();
+    if (b->op == 0) tr.m2m_unchecked(first, last);
+    if (b->op == 1) tr.m2l_unchecked(first, last);
+    if (b->op == 2) tr.l2l_unchecked(first, last);
+    auto t1 = std::chrono::steady_clock::now();
+    if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+    return 0;
+}
+
+void ref_mt_batch_destroy_d(void *h) { delete static_cast<MtBatch *>(h); }
 
 const char *ref_last_error() { return g_err; }
 

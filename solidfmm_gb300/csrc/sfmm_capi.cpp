@@ -669,6 +669,7 @@ int sfmm_bucket_by_order(sfmm_context *c, size_t n, const uint32_t *p_in, const 
     Range range("sfmm bucket");
     if (n == 0) return SFMM_OK;
     if (!p_in || !p_out || !order) return fail(c, SFMM_INVALID_ARG, "null device pointer");
+    if (n > 0xffffffffull) return fail(c, SFMM_INVALID_ARG, "batch larger than 2^32 - 1 translations");
     cudaSetDevice(c->device);
     cudaError_t e = c->d_work.ensure(bucket_work_words(c->P) * sizeof(uint32_t));
     if (e != cudaSuccess) return cuda_fail(c, e, "bucket workspace");

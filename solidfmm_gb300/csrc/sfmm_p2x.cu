@@ -294,7 +294,10 @@ __global__ void k_bucket_count(long long n, const uint32_t *pin, const uint32_t 
     }
 }
 
-// single CTA exclusive scan over K*K counters (K <= 33)
+// single CTA exclusive scan over nkeys counters, any number: thread t
+// handles a chunk of ceil(nkeys / 1024) consecutive keys.  Callers: the
+// context bucketing (K = P + 1 <= 87) and the allocation-free entry point
+// (K = max_order + 1 <= 87, 7 569 keys)
 __global__ void k_bucket_scan(uint32_t *cnt, int nkeys)
 {
     __shared__ uint32_t part[1024];
@@ -368,9 +371,33 @@ constexpr int kStaticBucketKeys = (kStaticBucketMaxOrder + 1) * (kStaticBucketMa
 
 __device__ __align__(256) uint32_t g_bucket_counters[kStaticBucketKeys];
 
-// device address of g_bucket_counters, looked up once per device
+// Device address of g_bucket_counters.  A __device__ array belongs to one CUDA
+// context (one per device with the runtime's primary contexts, but a caller
+// of the driver API may make another current, and cudaDeviceReset replaces
+// the primary one), so the address is looked up again on every call made
+// outside a stream capture and cached per current context for calls made
+// during a capture, when no lookup may load the module.
 std::mutex g_bucket_mtx;
-std::map<int, uint32_t *> g_bucket_addr;
+std::map<void *, uint32_t *> g_bucket_addr;
+
+using CtxGetCurrent = int (*)(void **);
+
+// the current CUcontext through the driver entry point (the library does not
+// link libcuda, so that it loads on machines without a GPU driver)
+void *current_context()
+{
+    static CtxGetCurrent fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGetCurrent>(f);
+    }();
+    void *ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
 
 }  // namespace
 
@@ -381,18 +408,26 @@ extern "C" int sfmm_bucket_by_order_noalloc(size_t n, const uint32_t *p_in, cons
     if (n > 0xffffffffull) return SFMM_INVALID_ARG;
     if (n == 0) return SFMM_OK;
     if (!p_in || !p_out || !order) return SFMM_INVALID_ARG;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return SFMM_CUDA_ERROR;
+    void *ctx = current_context();
+    if (!ctx) {  // no context current yet: initialise the current device's primary context
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) return SFMM_CUDA_ERROR;
+        ctx = current_context();
+    }
+    if (!ctx) return SFMM_CUDA_ERROR;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing((cudaStream_t)stream, &cap) != cudaSuccess) return SFMM_CUDA_ERROR;
     uint32_t *counters = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_bucket_mtx);
-        auto it = g_bucket_addr.find(dev);
-        if (it == g_bucket_addr.end()) {
+        if (cap == cudaStreamCaptureStatusNone) {
             // the host-side symbol is only a stand-in for the array; the
-            // kernels need its device address on this device
+            // kernels need its address in the current context
             if (cudaGetSymbolAddress((void **)&counters, g_bucket_counters) != cudaSuccess) return SFMM_CUDA_ERROR;
-            g_bucket_addr.emplace(dev, counters);
+            g_bucket_addr[ctx] = counters;
         } else {
+            auto it = g_bucket_addr.find(ctx);
+            if (it == g_bucket_addr.end()) return SFMM_INVALID_ARG;  // first call inside a capture
             counters = it->second;
         }
     }

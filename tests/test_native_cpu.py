@@ -12,7 +12,8 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+# the reference's own sources (test programs), where this machine has them
+REF = os.environ.get("SFMM_REF_SRC", "/root/reference")
 
 
 def _declared():
@@ -112,3 +113,32 @@ def test_reference_programs_compile_against_drop_in(native, prog, tmp_path):
                         f"-Wl,-rpath,{lib}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
     assert exe.exists()
+
+
+def test_drop_in_harmonics_match_reference_goldens(native, tmp_path):
+    """solidfmm::harmonics::R/S/dR/dS of the drop-in library against the
+    reference's own values at the golden points (solidfmm/harmonics.cpp:32-349,
+    generated by tests/golden/make_golden.py)."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "translations.npz"))
+    pts = g["harmonics/points"]
+    want = {k: g[f"harmonics/{k}"] for k in ("R", "S", "dR", "dS")}
+    S = want["R"].shape[1]
+    P = int(round((-1 + (1 + 4 * S) ** 0.5) / 2))
+    assert P * (P + 1) == S
+    lib = os.path.dirname(native._native.lib_path())
+    exe = tmp_path / "harmonics_check"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cxx", "harmonics_check.cpp"), "-o", str(exe), "-L", lib,
+                        "-lsfmm_gb300", f"-Wl,-rpath,{lib}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    args = [str(exe), str(P)] + [repr(float(v)) for v in pts.reshape(-1)]
+    out = np.frombuffer(subprocess.run(args, capture_output=True, check=True).stdout, dtype=np.float64)
+    per = 8 * S
+    assert out.size == per * len(pts)
+    for i in range(len(pts)):
+        row = out[i * per:(i + 1) * per]
+        got = {"R": row[:S], "S": row[S:2 * S], "dR": row[2 * S:5 * S], "dS": row[5 * S:]}
+        for k in got:
+            ref = want[k][i]
+            err = np.abs(got[k] - ref).max() / np.abs(ref).max()
+            assert err < 1e-13, (k, i, err)
