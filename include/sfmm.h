@@ -59,9 +59,25 @@ typedef enum { SFMM_M2M = 0, SFMM_M2L = 1, SFMM_L2L = 2 } sfmm_op;
  *           degree would take 30-bit mantissas past 1e-7.
  * SPLIT_FF: the same with float-float (double-FP32, ~2^-44 per operation)
  *           for every stage: relative error ~1e-13 at order 16.
- * The split modes need an SFMM_F64 context and orders <= 28 (FP32 exponent
- * range of the orthogonal-basis scale factors). */
-typedef enum { SFMM_PLAIN = 0, SFMM_SPLIT = 1, SFMM_SPLIT_FF = 2 } sfmm_precision;
+ * TC_TF32:  the tensor-core kernel (tcgen05, one thread per translation,
+ *           128 translations per MMA tile): every swap and z-translation is
+ *           an MMA against constant matrices held in shared memory, with both
+ *           operands split in two TF32 pieces (hi*hi + hi*lo + lo*hi, FP32
+ *           accumulation in tensor memory); FP64 geometry, FP32 rotations
+ *           and scaling, FP64 accumulation into the targets.  FP32-class
+ *           error (~1e-7 orthonormal).  Order bounds up to 16; batches with
+ *           a larger order bound run SFMM_SPLIT.
+ * TC_BF16:  the same kernel with BF16 pieces (kind::f16): ~16-bit operand
+ *           precision, error ~1e-5.
+ * The split and tensor-core modes need an SFMM_F64 context and orders <= 28
+ * (FP32 exponent range of the orthogonal-basis scale factors). */
+typedef enum {
+    SFMM_PLAIN = 0,
+    SFMM_SPLIT = 1,
+    SFMM_SPLIT_FF = 2,
+    SFMM_TC_TF32 = 3,
+    SFMM_TC_BF16 = 4
+} sfmm_precision;
 
 /* flags for the batch calls */
 enum {

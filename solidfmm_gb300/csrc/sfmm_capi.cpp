@@ -119,6 +119,13 @@ cudaError_t upload_offsets(sfmm_context *c)
 
 int ensure_tables(sfmm_context *c, Arith a)
 {
+    if (is_tc(a)) {
+        const int mode = a == Arith::TC32 ? 0 : 1;
+        if (c->tc[mode]) return SFMM_OK;
+        cudaError_t e = tc_prepare(&c->tc[mode], mode, c->host);
+        if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core table upload");
+        return SFMM_OK;
+    }
     DevTables &t = c->tab[(int)a];
     if (t.ready) return SFMM_OK;
     cudaError_t e = upload_offsets(c);
@@ -162,6 +169,12 @@ int arith_of(sfmm_context *c, int precision, Arith *out)
         *out = precision == SFMM_SPLIT ? Arith::FFQ : Arith::FF;
         return SFMM_OK;
     }
+    if (precision == SFMM_TC_TF32 || precision == SFMM_TC_BF16) {
+        if (c->dtype != SFMM_F64)
+            return fail(c, SFMM_UNSUPPORTED, "tensor-core precision needs an FP64 context (FP64 accumulation targets)");
+        *out = precision == SFMM_TC_TF32 ? Arith::TC32 : Arith::TC16;
+        return SFMM_OK;
+    }
     return fail(c, SFMM_INVALID_ARG, "unknown precision mode %d", precision);
 }
 
@@ -171,8 +184,11 @@ int arith_of(sfmm_context *c, int precision, Arith *out)
 // (about 1.35x per degree for M2M, in every arithmetic) pushes 30-bit
 // mantissas above 1e-7, and the batch runs in float-float instead.
 constexpr int kFixedM2MOrder = 18;
+// The tensor-core kernel holds a tile's expansions in tensor memory up to
+// order 16; batches with a larger order bound run the split kernel.
 Arith resolve_arith(Arith a, int op, int Pbound)
 {
+    if (is_tc(a) && Pbound > tc_max_order()) a = Arith::FFQ;
     if (a == Arith::FFQ && op == SFMM_M2M && Pbound > kFixedM2MOrder) return Arith::FF;
     return a;
 }
@@ -184,6 +200,17 @@ int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound, LaunchShape *sh
     std::lock_guard<std::mutex> lk(c->setup_mtx);
     int st = ensure_tables(c, a);
     if (st) return st;
+    if (is_tc(a)) {  // one 128-thread CTA per SM, one translation per thread
+        if (shape) {
+            *shape = LaunchShape{};
+            shape->G = 1;
+            shape->acc = 1;
+            shape->TS = 128;
+            shape->threads = 128;
+            shape->blocks_per_sm = 1;
+        }
+        return SFMM_OK;
+    }
     const auto key = std::make_pair((int)a, Pbound);
     auto it = c->shapes.find(key);
     if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound, default_group(a, Pbound))).first;
@@ -230,7 +257,6 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     LaunchShape s;
     int st = prepare_launch(c, op, a, Pbound, &s);
     if (st) return st;
-    const DevTables &t = c->tab[(int)a];
     KParams p{};
     p.op = op;
     p.P = Pbound;
@@ -254,6 +280,13 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.dst_ptr = dst_ptr;
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
     p.in_hbm = in_hbm ? 1 : 0;
+    if (is_tc(a)) {
+        cudaError_t e = launch_translate_tc(p, c->tc[a == Arith::TC32 ? 0 : 1], c->num_sms, stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core translation kernel launch");
+        c->launches++;
+        return SFMM_OK;
+    }
+    const DevTables &t = c->tab[(int)a];
     // swap blocks padded for this launch's group size (4 or 8 threads per
     // translation step 8 rows, one warp 32)
     const bool w8 = s.G != 32 && c->d_woff8;
@@ -446,6 +479,7 @@ void sfmm_destroy(sfmm_context *c)
     if (!c) return;
     cudaSetDevice(c->device);
     for (auto &t : c->tab) free_tables(t);
+    for (auto &t : c->tc) tc_release(t);
     for (int k = 0; k < 3; ++k) {
         c->d_src[k].release();
         c->d_dst[k].release();
@@ -516,6 +550,8 @@ int sfmm_set_group(sfmm_context *c, int precision, size_t order_bound, int group
     if (st) return st;
     if (order_bound > (size_t)c->P) return fail(c, SFMM_ORDER_RANGE, "order bound %zu exceeds the context order %d", order_bound, c->P);
     const int Pb = order_bound ? (int)order_bound : c->P;
+    if (is_tc(resolve_arith(a, SFMM_M2L, Pb)))
+        return fail(c, SFMM_UNSUPPORTED, "the tensor-core kernel runs one thread per translation");
     if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, SFMM_CUDA_ERROR, "cannot select device %d", c->device);
     LaunchShape s = best_shape(a, Pb, group);
     if (!s.acc) return fail(c, SFMM_INVALID_ARG, "no kernel runs %d threads per translation at order %d", group, Pb);
@@ -574,6 +610,24 @@ int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t
         return cuda_fail(c, e, "tuning setup");
     }
     a = resolve_arith(a, op, Pb);
+    if (is_tc(a)) {  // one launch shape: time it
+        float ms = 0;
+        for (int rep = 0; rep < 2 && st == SFMM_OK; ++rep) {
+            if (rep == 1 && (e = cudaEventRecord(e0, stream)) != cudaSuccess) break;
+            for (int k = 0; k < (rep ? 3 : 1) && st == SFMM_OK; ++k)
+                st = run_batch(c, stream, op, a, Pb, (long long)n, src, (long long)S, (long long)n, nullptr, dst,
+                               (long long)S, (long long)n, nullptr, d_ord, d_ord, d_shift, nullptr, 0);
+            if (rep == 1 && (e = cudaEventRecord(e1, stream)) != cudaSuccess) break;
+        }
+        if (st == SFMM_OK && e == cudaSuccess && (e = cudaEventSynchronize(e1)) == cudaSuccess)
+            e = cudaEventElapsedTime(&ms, e0, e1);
+        cleanup();
+        if (st != SFMM_OK) return st;
+        if (e != cudaSuccess) return cuda_fail(c, e, "tuning run");
+        if (group) *group = 1;
+        if (rate) *rate = ms > 0 ? 3.0 * (double)n / (ms * 1e-3) : 0.0;
+        return SFMM_OK;
+    }
     const auto key = std::make_pair((int)a, Pb);
     LaunchShape best;
     double best_rate = 0;

@@ -80,7 +80,8 @@ struct sfmm_context {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     sfmm::HostTables host;
-    sfmm::DevTables tab[4];  // indexed by Arith
+    sfmm::DevTables tab[sfmm::kNumArith];  // indexed by Arith (the tensor-core modes use tc[])
+    sfmm::TcDevTables *tc[2] = {nullptr, nullptr};  // tensor-core operand images, 3xTF32 / 3xBF16
     std::string err;
     std::atomic<uint64_t> launches{0};
     std::mutex mtx;  // serialises host-path calls (one translator object, one stream)

@@ -15,8 +15,11 @@ inline void clear_stale_error() { (void)cudaGetLastError(); }
 
 struct KParams;
 
-// FFQ: float-float with block fixed-point swaps and beta rotations
-enum class Arith { F64 = 0, F32 = 1, FF = 2, FFQ = 3 };
+// FFQ: float-float with block fixed-point swaps and beta rotations;
+// TC32 / TC16: the tensor-core kernel with 3xTF32 / 3xBF16 split products
+enum class Arith { F64 = 0, F32 = 1, FF = 2, FFQ = 3, TC32 = 4, TC16 = 5 };
+constexpr int kNumArith = 6;
+inline bool is_tc(Arith a) { return a == Arith::TC32 || a == Arith::TC16; }
 
 // Largest order the fused translation kernel supports: 4 threads per
 // translation up to 32, one warp per translation up to 96 (the reference's
@@ -46,6 +49,16 @@ LaunchShape best_shape(Arith a, int P, int G, bool small_tiles = false, int min_
 // Launch the fused translation kernel (defined in sfmm_k{64,32,ff,ffq}.cu).
 cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, int grid, cudaStream_t st);
 int translate_blocks_per_sm(Arith a, const LaunchShape &s);
+
+// Tensor-core translation kernel (sfmm_tc.cu): device images of the
+// constant matrices for one operand format (mode 0 = 3xTF32, 1 = 3xBF16),
+// built from the context's host tables for degrees below min(P, 16).
+struct HostTables;
+struct TcDevTables;
+cudaError_t tc_prepare(TcDevTables **out, int mode, const HostTables &host);
+void tc_release(TcDevTables *t);
+int tc_max_order();
+cudaError_t launch_translate_tc(const KParams &p, const TcDevTables *t, int num_sms, cudaStream_t st);
 
 // P2M / P2L (sfmm_p2x.cu)
 // expansion j takes particles [j nq, (j+1) nq), or [offset[j], offset[j+1]) with an offset array
