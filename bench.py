@@ -213,13 +213,14 @@ def accuracy(ctx, op, P, src, shift, pin, nsub, dev):
                    sh.cpu().numpy())
     w = norm_weights(P, "M" if op == "m2m" else "L")
     out = {}
-    for name, prec in (("plain_fp64", 0), ("split", 1), ("split_ff", 2)):
+    for name, prec in (("plain_fp64", 0), ("split", 1), ("split_ff", 2), ("tc_tf32x3", 3), ("tc_bf16x3", 4)):
         d = torch.zeros(nsub, S, dtype=torch.float64, device=dev)
         ctx.translate_device(op, prec, nsub, s, S, nsub, d, S, nsub, pi, pi, sh)
         torch.cuda.synchronize()
         got = d.cpu().numpy()
         out[name] = {"rel_l2_orthonormal_max": rel_err(got, ref, w), "rel_l2_raw_max": rel_err(got, ref),
-                     "rel_l2_orthonormal_per_degree_max": per_degree_err(got, ref, P, w)}
+                     "rel_l2_orthonormal_per_degree_max": per_degree_err(got, ref, P, w),
+                     "rel_l2_raw_per_degree_max": per_degree_err(got, ref, P)}
     return out
 
 
@@ -736,6 +737,11 @@ def main():
     ms_split, launches, clk = timed(1, args.steps, args.warmup, clocks)
     ms_plain, _, _ = timed(0, max(2, args.steps // 2), 1)
     ms_ff, _, _ = timed(2, max(2, args.steps // 2), 1)
+    tc_ms = {}
+    tc_clk = {}
+    if P <= 16:  # the tensor-core kernel's order range
+        for name, prec in (("tc_tf32x3", 3), ("tc_bf16x3", 4)):
+            tc_ms[name], _, tc_clk[name] = timed(prec, max(3, args.steps // 2), 2, Clocks(local))
     value = world * N / (ms_split * 1e-3)
     plain_value = world * N / (ms_plain * 1e-3)
     ff_value = world * N / (ms_ff * 1e-3)
@@ -797,24 +803,46 @@ def main():
             hbm_peak = json.load(f).get("hbm_gbs", hbm_peak)
         peak_src = "measured"
     tb = TRAFFIC.get((op, P))
-    roof = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved_gbs / hbm_peak, "traffic": tb * N if tb else None,
+    # t_roof = max over the bounds of the work the kernel must do: HBM bytes,
+    # useful flops on the FP64 pipe (none in split), on the FP32/INT pipes
+    # (all of split's), on the tensor pipe (none in split)
+    t_hbm = B / (hbm_peak * 1e9)
+    t_fp32 = F / peaks["fp32"]
+    t_roof = max(t_hbm, t_fp32)
+    roof = {"bound": "hbm" if t_hbm >= t_fp32 else "fp32", "achieved": achieved_gbs, "peak": hbm_peak,
+            "unit": "GB/s", "frac": t_roof / t_kernel, "traffic": tb * N if tb else None,
             "traffic_source": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the split kernel, "
                                f"{tb:.0f} B per translation on 65 536 translations, scaled to {N}") if tb else None,
             "peak_source": peak_src, "kernel": "k_translate<ff, G, ACC, fixed, in HBM> (split)",
-            "bytes_per_translation": B,
-            "binding": "instruction issue on the FP32/INT pipes, not HBM (DRAM traffic equals the algorithmic "
-                       "bytes): see roofline_issue"}
-    roof_issue = None
+            "bytes_per_translation": B, "useful_flops_per_translation": F,
+            "t_roof_ns_per_translation": {"hbm": t_hbm * 1e9, "fp32_pipe": t_fp32 * 1e9, "fp64_pipe": 0.0,
+                                          "tensor_pipe": 0.0},
+            "frac_definition": "t_roof / t_measured, t_roof = max(bytes / HBM peak, useful FP32-pipe flops / "
+                               "measured FFMA peak) per translation"}
+    issue_util = None
     ipt = INSTRUCTIONS.get((op, P))
     if ipt and clk and clk.get("sm_mhz"):
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         peak_issue = sms * 4 * clk["sm_mhz"] * 1e6
-        roof_issue = {"bound": "instruction issue", "unit": "warp instructions/s",
+        issue_util = {"what": "issue-slot utilisation of the split kernel (a diagnostic, not a roofline: the "
+                              "instructions counted include the emulation around the useful work)",
                       "instructions_per_translation": ipt, "achieved": ipt / t_kernel, "peak": peak_issue,
                       "frac": ipt / t_kernel / peak_issue,
                       "peak_source": f"{sms} SMs x 4 schedulers x 1 instruction/cycle at the sampled {clk['sm_mhz']} MHz",
                       "instructions_source": "ncu smsp__inst_executed.sum of the split kernel / 65 536 translations"}
+    tc_rows = {}
+    for name, ms in tc_ms.items():
+        tk = ms * 1e-3 / N
+        row = {"value": world * N / (ms * 1e-3), "unit": "translations/s", "ms_per_step": ms,
+               "over_plain_fp64": (world * N / (ms * 1e-3)) / plain_value,
+               "over_split": (world * N / (ms * 1e-3)) / value,
+               "roofline": {"bound": "hbm", "frac": t_hbm / tk, "achieved_gbs": B / tk / 1e9,
+                            "peak": hbm_peak, "note": "t_roof = bytes / HBM peak (the tensor and FP32 pipes need "
+                                                      "far less time for the useful work)"},
+               "clocks": tc_clk.get(name)}
+        if acc and name in acc:
+            row["accuracy_vs_fp64_oracle_1000"] = acc[name]
+        tc_rows[name] = row
     # the split path does FP64-class work on the FP32 and integer pipes: its
     # useful flop rate set against the FP64 pipe's measured peak (a ratio
     # above 1 is beyond any FP64 kernel's reach)
@@ -854,7 +882,13 @@ def main():
                                  "api": "sfmm_translate_host: arrays of N source and target solid addresses (the "
                                         "drop-in classic and multithreaded_translator calls), in place over the "
                                         "host link"},
-            "roofline": roof, "roofline_issue": roof_issue, "roofline_compute": roof_compute,
+            "tensor_core": tc_rows or None,
+            "tensor_core_note": "tcgen05 kernel, one thread per translation, 128 translations per MMA tile: swaps "
+                                "and z-translations as M=128 N=K=16 MMAs with operands split in two pieces "
+                                "(hi*hi+hi*lo+lo*hi, FP32 accumulation in tensor memory); FP32-class error, above "
+                                "the 1e-7 contract, so the headline value stays the split kernel",
+            "split_m2m_note": "split M2M batches with an order bound above 18 run float-float",
+            "roofline": roof, "issue_utilisation": issue_util, "roofline_compute": roof_compute,
             "roofline_plain_fp64": roof_fp64,
             "cpu_baseline": cpu, "cpu_baseline_port": cpu_port, "clocks": clk, "gpu_launches": launches}
     print(json.dumps(line))
