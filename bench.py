@@ -213,7 +213,7 @@ def accuracy(ctx, op, P, src, shift, pin, nsub, dev):
                    sh.cpu().numpy())
     w = norm_weights(P, "M" if op == "m2m" else "L")
     out = {}
-    for name, prec in (("plain_fp64", 0), ("split", 1), ("split_ff", 2), ("tc_tf32x3", 3), ("tc_bf16x3", 4)):
+    for name, prec in (("plain_fp64", 0), ("split", 1), ("split_ff", 2), ("tc_tf32x3", 3), ("tc_bf16x3", 4), ("tc_bf16x6", 5)):
         d = torch.zeros(nsub, S, dtype=torch.float64, device=dev)
         ctx.translate_device(op, prec, nsub, s, S, nsub, d, S, nsub, pi, pi, sh)
         torch.cuda.synchronize()
@@ -740,7 +740,7 @@ def main():
     tc_ms = {}
     tc_clk = {}
     if P <= 16:  # the tensor-core kernel's order range
-        for name, prec in (("tc_tf32x3", 3), ("tc_bf16x3", 4)):
+        for name, prec in (("tc_tf32x3", 3), ("tc_bf16x3", 4), ("tc_bf16x6", 5)):
             tc_ms[name], _, tc_clk[name] = timed(prec, max(3, args.steps // 2), 2, Clocks(local))
     value = world * N / (ms_split * 1e-3)
     plain_value = world * N / (ms_plain * 1e-3)
@@ -884,9 +884,10 @@ def main():
                                         "host link"},
             "tensor_core": tc_rows or None,
             "tensor_core_note": "tcgen05 kernel, one thread per translation, 128 translations per MMA tile: swaps "
-                                "and z-translations as M=128 N=K=16 MMAs with operands split in two pieces "
-                                "(hi*hi+hi*lo+lo*hi, FP32 accumulation in tensor memory); FP32-class error, above "
-                                "the 1e-7 contract, so the headline value stays the split kernel",
+                                "and z-translations as M=128 N=K=16 MMAs with operands split in two (3xTF32, "
+                                "3xBF16) or three (BF16x6) pieces, FP32 accumulation in tensor memory; the "
+                                "accumulator's rounding per MMA stage keeps every mode above the 1e-7 contract, so "
+                                "the headline value stays the split kernel",
             "split_m2m_note": "split M2M batches with an order bound above 18 run float-float",
             "roofline": roof, "issue_utilisation": issue_util, "roofline_compute": roof_compute,
             "roofline_plain_fp64": roof_fp64,

@@ -69,6 +69,10 @@ typedef enum { SFMM_M2M = 0, SFMM_M2L = 1, SFMM_L2L = 2 } sfmm_op;
  *           a larger order bound run SFMM_SPLIT.
  * TC_BF16:  the same kernel with BF16 pieces (kind::f16): ~16-bit operand
  *           precision, error ~1e-5.
+ * TC_BF16X6: the same kernel with three BF16 pieces per operand (the six
+ *           products whose piece indices sum to at most 2, smallest first)
+ *           and float-float edge scaling: each MMA stage rounds about once
+ *           in FP32.
  * The split and tensor-core modes need an SFMM_F64 context and orders <= 28
  * (FP32 exponent range of the orthogonal-basis scale factors). */
 typedef enum {
@@ -76,7 +80,8 @@ typedef enum {
     SFMM_SPLIT = 1,
     SFMM_SPLIT_FF = 2,
     SFMM_TC_TF32 = 3,
-    SFMM_TC_BF16 = 4
+    SFMM_TC_BF16 = 4,
+    SFMM_TC_BF16X6 = 5
 } sfmm_precision;
 
 /* flags for the batch calls */

@@ -15,7 +15,7 @@ from . import build as _build
 
 F32, F64 = 0, 1
 M2M, M2L, L2L = 0, 1, 2
-PLAIN, SPLIT, SPLIT_FF, TC_TF32, TC_BF16 = 0, 1, 2, 3, 4
+PLAIN, SPLIT, SPLIT_FF, TC_TF32, TC_BF16, TC_BF16X6 = 0, 1, 2, 3, 4, 5
 TARGETS_UNIQUE, TARGETS_REPEAT = 0, 1
 OPS = {"m2m": M2M, "m2l": M2L, "l2l": L2L}
 

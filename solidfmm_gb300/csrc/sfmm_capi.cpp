@@ -120,7 +120,7 @@ cudaError_t upload_offsets(sfmm_context *c)
 int ensure_tables(sfmm_context *c, Arith a)
 {
     if (is_tc(a)) {
-        const int mode = a == Arith::TC32 ? 0 : 1;
+        const int mode = tc_mode(a);
         if (c->tc[mode]) return SFMM_OK;
         cudaError_t e = tc_prepare(&c->tc[mode], mode, c->host);
         if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core table upload");
@@ -169,10 +169,10 @@ int arith_of(sfmm_context *c, int precision, Arith *out)
         *out = precision == SFMM_SPLIT ? Arith::FFQ : Arith::FF;
         return SFMM_OK;
     }
-    if (precision == SFMM_TC_TF32 || precision == SFMM_TC_BF16) {
+    if (precision == SFMM_TC_TF32 || precision == SFMM_TC_BF16 || precision == SFMM_TC_BF16X6) {
         if (c->dtype != SFMM_F64)
             return fail(c, SFMM_UNSUPPORTED, "tensor-core precision needs an FP64 context (FP64 accumulation targets)");
-        *out = precision == SFMM_TC_TF32 ? Arith::TC32 : Arith::TC16;
+        *out = precision == SFMM_TC_TF32 ? Arith::TC32 : (precision == SFMM_TC_BF16 ? Arith::TC16 : Arith::TC16X6);
         return SFMM_OK;
     }
     return fail(c, SFMM_INVALID_ARG, "unknown precision mode %d", precision);
@@ -281,7 +281,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
     p.in_hbm = in_hbm ? 1 : 0;
     if (is_tc(a)) {
-        cudaError_t e = launch_translate_tc(p, c->tc[a == Arith::TC32 ? 0 : 1], c->num_sms, stream);
+        cudaError_t e = launch_translate_tc(p, c->tc[tc_mode(a)], c->num_sms, stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core translation kernel launch");
         c->launches++;
         return SFMM_OK;

@@ -81,7 +81,7 @@ struct sfmm_context {
     cudaStream_t stream = nullptr;
     sfmm::HostTables host;
     sfmm::DevTables tab[sfmm::kNumArith];  // indexed by Arith (the tensor-core modes use tc[])
-    sfmm::TcDevTables *tc[2] = {nullptr, nullptr};  // tensor-core operand images, 3xTF32 / 3xBF16
+    sfmm::TcDevTables *tc[3] = {nullptr, nullptr, nullptr};  // tensor-core operand images by format
     std::string err;
     std::atomic<uint64_t> launches{0};
     std::mutex mtx;  // serialises host-path calls (one translator object, one stream)

@@ -16,10 +16,13 @@ inline void clear_stale_error() { (void)cudaGetLastError(); }
 struct KParams;
 
 // FFQ: float-float with block fixed-point swaps and beta rotations;
-// TC32 / TC16: the tensor-core kernel with 3xTF32 / 3xBF16 split products
-enum class Arith { F64 = 0, F32 = 1, FF = 2, FFQ = 3, TC32 = 4, TC16 = 5 };
-constexpr int kNumArith = 6;
-inline bool is_tc(Arith a) { return a == Arith::TC32 || a == Arith::TC16; }
+// TC32 / TC16 / TC16X6: the tensor-core kernel with 3xTF32 / 3xBF16 /
+// BF16x6 split products
+enum class Arith { F64 = 0, F32 = 1, FF = 2, FFQ = 3, TC32 = 4, TC16 = 5, TC16X6 = 6 };
+constexpr int kNumArith = 7;
+inline bool is_tc(Arith a) { return a == Arith::TC32 || a == Arith::TC16 || a == Arith::TC16X6; }
+// operand format of a tensor-core arithmetic (sfmm_tc.cu)
+inline int tc_mode(Arith a) { return a == Arith::TC32 ? 0 : (a == Arith::TC16 ? 1 : 2); }
 
 // Largest order the fused translation kernel supports: 4 threads per
 // translation up to 32, one warp per translation up to 96 (the reference's
@@ -51,7 +54,8 @@ cudaError_t launch_translate(Arith a, const KParams &p, const LaunchShape &s, in
 int translate_blocks_per_sm(Arith a, const LaunchShape &s);
 
 // Tensor-core translation kernel (sfmm_tc.cu): device images of the
-// constant matrices for one operand format (mode 0 = 3xTF32, 1 = 3xBF16),
+// constant matrices for one operand format (mode 0 = 3xTF32, 1 = 3xBF16,
+// 2 = BF16x6),
 // built from the context's host tables for degrees below min(P, 16).
 struct HostTables;
 struct TcDevTables;

@@ -48,22 +48,26 @@ float bf16_float(uint16_t h)
     return f;
 }
 
+int pieces_of(int mode) { return mode == 2 ? 3 : 2; }
+
 // Entry (r, k) of a 16 x 16 B operand (K-major core matrices) in format
-// `mode`: piece 0 (hi) at img, piece 1 (lo) at img + image size.
+// `mode`: piece i at img + i * image size, each piece the rounding of what the
+// earlier ones left of v (computed in FP64).
 void put_b(unsigned char *img, int mode, int r, int k, double v)
 {
     const int esz = mode == 0 ? 4 : 2, KC = 16 * esz / 16, ib = 16 * 16 * esz;
     const size_t off = (size_t)((r / 8) * KC + (k * esz) / 16) * 128 + (r % 8) * 16 + (k * esz) % 16;
-    if (mode == 0) {
-        const float hi = tf32_rna_host((float)v);
-        const float lo = tf32_rna_host((float)(v - (double)hi));
-        std::memcpy(img + off, &hi, 4);
-        std::memcpy(img + ib + off, &lo, 4);
-    } else {
-        const uint16_t hi = bf16_rn_host((float)v);
-        const uint16_t lo = bf16_rn_host((float)(v - (double)bf16_float(hi)));
-        std::memcpy(img + off, &hi, 2);
-        std::memcpy(img + ib + off, &lo, 2);
+    double rem = v;
+    for (int i = 0; i < pieces_of(mode); ++i) {
+        if (mode == 0) {
+            const float pc = tf32_rna_host((float)rem);
+            std::memcpy(img + i * ib + off, &pc, 4);
+            rem -= (double)pc;
+        } else {
+            const uint16_t pc = bf16_rn_host((float)rem);
+            std::memcpy(img + i * ib + off, &pc, 2);
+            rem -= (double)bf16_float(pc);
+        }
     }
 }
 
@@ -82,7 +86,7 @@ constexpr int kTcGroups = 4;
 template <int MODE>
 int smem_bytes(int P)
 {
-    const TcSmem sm(P, TcLayout<MODE>::IMG_A, TcLayout<MODE>::IMG_B);
+    const TcSmem sm = TcSmem::of<MODE>(P);
     // at least 116 KB: two CTAs never share an SM (each allocates all of
     // its tensor memory)
     return sm.total < 116 * 1024 ? 116 * 1024 : sm.total;
@@ -124,16 +128,17 @@ cudaError_t tc_prepare(TcDevTables **out, int mode, const HostTables &host)
     t->Pt = host.P < kTcMaxOrder ? host.P : kTcMaxOrder;
     const int Pt = t->Pt;
     const int ib = mode == 0 ? TcLayout<0>::IMG_B : TcLayout<1>::IMG_B;
+    const int np = pieces_of(mode);  // group image: [part][piece] (swaps), [piece] (z)
     std::vector<unsigned char> W, H[3];
     for (int P = 1; P <= Pt; ++P) {
         t->offW[P] = W.size();
         t->offH[P] = H[0].size();
         const int NG = tc_deg_groups(P), NZ = tc_z_groups(P);
-        W.resize(W.size() + (size_t)NG * 4 * ib, 0);
+        W.resize(W.size() + (size_t)NG * 2 * np * ib, 0);
         for (int g = 0; g < NG; ++g) {
             const TcGroup gr = tc_deg_group(P, g);
             for (int part = 0; part < 2; ++part) {
-                unsigned char *img = &W[t->offW[P] + ((size_t)g * 4 + part * 2) * ib];
+                unsigned char *img = &W[t->offW[P] + ((size_t)g * 2 + part) * np * ib];
                 for (int blk = 0; blk < 2; ++blk) {
                     const int n = blk ? gr.n2 : gr.n1, d = blk ? gr.d2 : gr.d1, o = blk ? gr.d1 : 0;
                     for (int i = 0; i < d; ++i)
@@ -142,10 +147,10 @@ cudaError_t tc_prepare(TcDevTables **out, int mode, const HostTables &host)
             }
         }
         for (int op = 0; op < 3; ++op) {
-            H[op].resize(H[op].size() + (size_t)NZ * 2 * ib, 0);
+            H[op].resize(H[op].size() + (size_t)NZ * np * ib, 0);
             for (int g = 0; g < NZ; ++g) {
                 const TcGroup gr = tc_z_group(P, g);
-                unsigned char *img = &H[op][t->offH[P] + (size_t)g * 2 * ib];
+                unsigned char *img = &H[op][t->offH[P] + (size_t)g * np * ib];
                 for (int blk = 0; blk < 2; ++blk) {
                     const int m = blk ? gr.n2 : gr.n1, L = blk ? gr.d2 : gr.d1, o = blk ? gr.d1 : 0;
                     if (!L) continue;
@@ -162,16 +167,22 @@ cudaError_t tc_prepare(TcDevTables **out, int mode, const HostTables &host)
     const std::vector<double> *ev[4] = {&host.e_in_M, &host.e_in_L, &host.e_out_L, &host.e_out_M};
     cudaError_t e = upload_vec(&t->W, W);
     for (int op = 0; op < 3 && e == cudaSuccess; ++op) e = upload_vec(&t->H[op], H[op]);
+    // edge factors in FP32; the float-float-edge format keeps the low words
+    // after a fixed stride of 136 (order 16)
+    const size_t kNE = (size_t)kTcMaxOrder * (kTcMaxOrder + 1) / 2;
     for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
-        std::vector<float> f(ne);
-        for (size_t i = 0; i < ne; ++i) f[i] = (float)(*ev[k])[i];
+        std::vector<float> f(mode == 2 ? 2 * kNE : ne, 0.f);
+        for (size_t i = 0; i < ne; ++i) {
+            f[i] = (float)(*ev[k])[i];
+            if (mode == 2) f[kNE + i] = (float)((*ev[k])[i] - (double)f[i]);
+        }
         e = upload_vec(&t->e[k], f);
     }
     if (e == cudaSuccess) {
-        const int smax = mode == 0 ? smem_bytes<0>(Pt) : smem_bytes<1>(Pt);
-        e = mode == 0
-                ? cudaFuncSetAttribute(k_translate_tc<0, kTcGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax)
-                : cudaFuncSetAttribute(k_translate_tc<1, kTcGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        if (mode == 0) e = cudaFuncSetAttribute(k_translate_tc<0, kTcGroups>, at, smem_bytes<0>(Pt));
+        else if (mode == 1) e = cudaFuncSetAttribute(k_translate_tc<1, kTcGroups>, at, smem_bytes<1>(Pt));
+        else e = cudaFuncSetAttribute(k_translate_tc<2, kTcGroups>, at, smem_bytes<2>(Pt));
     }
     if (e != cudaSuccess) {
         tc_release(t);
@@ -196,10 +207,11 @@ cudaError_t launch_translate_tc(const KParams &p, const TcDevTables *t, int num_
     tt.wait_limit = 1u << 22;
     const long long tiles = (p.n + kTcRows - 1) / kTcRows;
     const int grid = (int)(tiles < num_sms ? tiles : num_sms);
-    const int smem = t->mode == 0 ? smem_bytes<0>(p.P) : smem_bytes<1>(p.P);
+    const int nt = kTcRows * kTcGroups;
     clear_stale_error();
-    if (t->mode == 0) k_translate_tc<0, kTcGroups><<<grid, kTcRows * kTcGroups, smem, st>>>(p, tt);
-    else k_translate_tc<1, kTcGroups><<<grid, kTcRows * kTcGroups, smem, st>>>(p, tt);
+    if (t->mode == 0) k_translate_tc<0, kTcGroups><<<grid, nt, smem_bytes<0>(p.P), st>>>(p, tt);
+    else if (t->mode == 1) k_translate_tc<1, kTcGroups><<<grid, nt, smem_bytes<1>(p.P), st>>>(p, tt);
+    else k_translate_tc<2, kTcGroups><<<grid, nt, smem_bytes<2>(p.P), st>>>(p, tt);
     return cudaGetLastError();
 }
 

@@ -91,7 +91,11 @@ __host__ __device__ inline int tc_state_col(int P, int n, int m)
     return g * P + (m == g ? 0 : P - g) + (n - m);
 }
 
-// Operand formats: 0 = 3xTF32, 1 = 3xBF16.
+// Operand formats: 0 = 3xTF32, 1 = 3xBF16 (two pieces per operand, the three
+// products hi*hi + hi*lo + lo*hi), 2 = BF16x6 (three BF16 pieces per operand,
+// the six products whose pieces sum to at most 2, issued smallest first so
+// that the FP32 accumulator rounds the sum about once; the edges of this
+// mode run in float-float and feed the split directly).
 template <int MODE>
 struct TcFmt;
 template <>
@@ -99,6 +103,8 @@ struct TcFmt<0> {
     static constexpr int ESZ = 4;
     static constexpr int KC = 4;      // core matrices along K = 16
     static constexpr int KSTEPS = 2;  // MMA instructions along K (K = 8 each)
+    static constexpr int PIECES = 2;
+    static constexpr bool FF = false;  // float-float edges
     static constexpr uint32_t FMT = tc::FMT_TF32;
 };
 template <>
@@ -106,6 +112,17 @@ struct TcFmt<1> {
     static constexpr int ESZ = 2;
     static constexpr int KC = 2;
     static constexpr int KSTEPS = 1;  // K = 16 in one instruction
+    static constexpr int PIECES = 2;
+    static constexpr bool FF = false;
+    static constexpr uint32_t FMT = tc::FMT_BF16;
+};
+template <>
+struct TcFmt<2> {
+    static constexpr int ESZ = 2;
+    static constexpr int KC = 2;
+    static constexpr int KSTEPS = 1;
+    static constexpr int PIECES = 3;
+    static constexpr bool FF = true;
     static constexpr uint32_t FMT = tc::FMT_BF16;
 };
 
@@ -114,7 +131,11 @@ struct TcLayout {
     static constexpr int IMG_A = kTcRows * kTcNodes * TcFmt<MODE>::ESZ;  // one piece of one part
     static constexpr int IMG_B = kTcNodes * kTcNodes * TcFmt<MODE>::ESZ;
     static constexpr int SBO = TcFmt<MODE>::KC * 128;
-    static constexpr int SLOT = 4 * IMG_A;  // A operand of one group: [part][piece]
+    static constexpr int PART_A = TcFmt<MODE>::PIECES * IMG_A;  // A operand of one part: [piece]
+    static constexpr int SLOT = 2 * PART_A;                     // A operand of one group: [part][piece]
+    static constexpr int PART_B = TcFmt<MODE>::PIECES * IMG_B;  // B operand of one part: [piece]
+    static constexpr int GRP_W = 2 * PART_B;                    // swap group: [part][piece]
+    static constexpr int GRP_H = PART_B;                        // z group: [piece] (both parts)
 };
 
 // Kernel arguments beyond the translation batch: the B images of this
@@ -122,35 +143,42 @@ struct TcLayout {
 struct TcTables {
     const unsigned char *W;  // [swap group][part][piece] images
     const unsigned char *H;  // [z group][piece] images
-    const float *ein, *eout;  // edge factors of this op, n(n+1)/2 + m, n < 16
+    const float *ein, *eout;  // edge factors of this op, n(n+1)/2 + m, n < 16 (float-float pairs
+                              // for the float-float-edge formats)
     uint32_t wait_limit;      // mbarrier polls before a wait is declared failed
 };
 
-// shared-memory plan of one CTA (byte offsets), for order bound P
+// shared-memory plan of one CTA (byte offsets), for order bound P and
+// operand format MODE
 struct TcSmem {
     int w, h, a, pw, rp, ein, eout, bar, total;
-    __host__ __device__ TcSmem(int P, int img_a, int img_b)
+    template <int MODE>
+    __host__ __device__ static TcSmem of(int P)
     {
+        using L = TcLayout<MODE>;
+        constexpr int ff = TcFmt<MODE>::FF ? 2 : 1;  // hi (and lo) words per value
+        TcSmem s;
         int o = 0;
-        w = o;
-        o += tc_deg_groups(P) * 4 * img_b;
-        h = o;
-        o += tc_z_groups(P) * 2 * img_b;
-        a = o;  // three A slots: a group's operand is written two steps after the
-                // previous occupant's last MMA was issued, which by then has completed
-        o += 3 * 4 * img_a;
-        pw = o;  // cos/sin m alpha, cos/sin m beta: [4][m][thread]
-        o += 4 * kTcMaxOrder * kTcRows * 4;
-        rp = o;  // forward and backward r-power of degree n: [2][n][thread]
-        o += 2 * kTcMaxOrder * kTcRows * 4;
-        ein = o;
-        o += kTcMaxOrder * (kTcMaxOrder + 1) / 2 * 4;
-        eout = o;
-        o += kTcMaxOrder * (kTcMaxOrder + 1) / 2 * 4;
+        s.w = o;
+        o += tc_deg_groups(P) * L::GRP_W;
+        s.h = o;
+        o += tc_z_groups(P) * L::GRP_H;
+        s.a = o;  // three A slots: a group's operand is written two steps after the
+                  // previous occupant's last MMA was issued, which by then has completed
+        o += 3 * L::SLOT;
+        s.pw = o;  // cos/sin m alpha, cos/sin m beta (hi, then lo): [word][m][thread]
+        o += 4 * ff * kTcMaxOrder * kTcRows * 4;
+        s.rp = o;  // forward and backward r-power of degree n (hi, then lo): [word][n][thread]
+        o += 2 * ff * kTcMaxOrder * kTcRows * 4;
+        s.ein = o;
+        o += ff * kTcMaxOrder * (kTcMaxOrder + 1) / 2 * 4;
+        s.eout = o;
+        o += ff * kTcMaxOrder * (kTcMaxOrder + 1) / 2 * 4;
         o = (o + 15) & ~15;
-        bar = o;
+        s.bar = o;
         o += 48;  // four mbarriers + tensor-memory address
-        total = o;
+        s.total = o;
+        return s;
     }
 };
 
@@ -174,69 +202,38 @@ __device__ __forceinline__ float f32_from_d(double x)
     return __uint_as_float(b | (hw & 0x80000000u));
 }
 
-// Row `t` of the split A operand: pieces hi and lo of v[0..15] into the two
-// images at `img` (piece 0) and `img + IMG_A` (piece 1).
+// D (+)= A * B^T over the split products of one part: A pieces at
+// a + i IMG_A, B pieces at b + j IMG_B, products (i, j) with i + j below the
+// piece count, the smallest first (they sum almost exactly before the
+// largest, hi*hi, is added: the FP32 accumulator then rounds about once).
 template <int MODE>
-__device__ __forceinline__ void put_row(unsigned char *img, int t, const float (&v)[16])
+__device__ __forceinline__ void mma_part(uint32_t dt, uint32_t a, uint32_t b)
 {
-    constexpr int IA = TcLayout<MODE>::IMG_A;
-    unsigned char *r0 = img + (t >> 3) * TcFmt<MODE>::KC * 128 + (t & 7) * 16;
-    if constexpr (MODE == 0) {
+    using L = TcLayout<MODE>;
+    constexpr uint32_t ID = tc::idesc(TcFmt<MODE>::FMT, kTcRows, kTcNodes);
+    constexpr int NP = TcFmt<MODE>::PIECES == 3 ? 6 : 3;
+    constexpr int pi[6] = {2, 1, 0, 1, 0, 0}, pj[6] = {0, 1, 2, 0, 1, 0};  // 3 pieces
+    constexpr int qi[3] = {1, 0, 0}, qj[3] = {0, 1, 0};                    // 2 pieces
 #pragma unroll
-        for (int kc = 0; kc < 4; ++kc) {
-            float h[4], l[4];
+    for (int p = 0; p < NP; ++p) {
+        const int i = NP == 6 ? pi[p] : qi[p], j = NP == 6 ? pj[p] : qj[p];
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                h[e] = tf32_rna(v[4 * kc + e]);
-                l[e] = tf32_rna(v[4 * kc + e] - h[e]);
-            }
-            *reinterpret_cast<float4 *>(r0 + kc * 128) = make_float4(h[0], h[1], h[2], h[3]);
-            *reinterpret_cast<float4 *>(r0 + IA + kc * 128) = make_float4(l[0], l[1], l[2], l[3]);
-        }
-    } else {
-#pragma unroll
-        for (int kc = 0; kc < 2; ++kc) {
-            uint32_t h[4], l[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const float a = v[8 * kc + 2 * e], b = v[8 * kc + 2 * e + 1];
-                const __nv_bfloat162 hb = __floats2bfloat162_rn(a, b);
-                const __nv_bfloat162 lb = __floats2bfloat162_rn(a - __low2float(hb), b - __high2float(hb));
-                h[e] = *reinterpret_cast<const uint32_t *>(&hb);
-                l[e] = *reinterpret_cast<const uint32_t *>(&lb);
-            }
-            *reinterpret_cast<uint4 *>(r0 + kc * 128) = make_uint4(h[0], h[1], h[2], h[3]);
-            *reinterpret_cast<uint4 *>(r0 + IA + kc * 128) = make_uint4(l[0], l[1], l[2], l[3]);
+        for (int c = 0; c < TcFmt<MODE>::KSTEPS; ++c) {
+            const uint64_t da = tc::sdesc(a + i * L::IMG_A + c * 256, 128, L::SBO);
+            const uint64_t db = tc::sdesc(b + j * L::IMG_B + c * 256, 128, L::SBO);
+            if constexpr (MODE == 0) tc::mma_tf32(dt, da, db, ID, (p | c) != 0);
+            else tc::mma_f16(dt, da, db, ID, (p | c) != 0);
         }
     }
 }
 
-// D (+)= A * B^T over the three split products, for one part: A images at
-// a (hi) and a + IMG_A (lo), B images at b (hi) and b + IMG_B (lo).
-template <int MODE>
-__device__ __forceinline__ void mma3(uint32_t dt, uint32_t a, uint32_t b)
-{
-    constexpr int IA = TcLayout<MODE>::IMG_A, IB = TcLayout<MODE>::IMG_B, SBO = TcLayout<MODE>::SBO;
-    constexpr uint32_t ID = tc::idesc(TcFmt<MODE>::FMT, kTcRows, kTcNodes);
-    const uint32_t pa[3] = {0u, 0u, (uint32_t)IA}, pb[3] = {0u, (uint32_t)IB, 0u};
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-        for (int c = 0; c < TcFmt<MODE>::KSTEPS; ++c) {
-            const uint64_t da = tc::sdesc(a + pa[p] + c * 256, 128, SBO);
-            const uint64_t db = tc::sdesc(b + pb[p] + c * 256, 128, SBO);
-            if constexpr (MODE == 0) tc::mma_tf32(dt, da, db, ID, (p | c) != 0);
-            else tc::mma_f16(dt, da, db, ID, (p | c) != 0);
-        }
-}
-
-// both parts of one group: A slot at a, B images at b (real part pieces
-// at b, b + IMG_B; imaginary part at b + boff, b + boff + IMG_B), D at dt
+// both parts of one group: A slot at a, B images at b (real part) and
+// b + boff (imaginary part), D at dt (real) and dt + 16 (imaginary)
 template <int MODE>
 __device__ __forceinline__ void mma_group(uint32_t dt, uint32_t a, uint32_t b, uint32_t boff)
 {
-    mma3<MODE>(dt, a, b);
-    mma3<MODE>(dt + 16, a + 2 * TcLayout<MODE>::IMG_A, b + boff);
+    mma_part<MODE>(dt, a, b);
+    mma_part<MODE>(dt + 16, a + TcLayout<MODE>::PART_A, b + boff);
 }
 
 // Tie registers written by tcgen05.ld to the preceding tcgen05.wait::ld:
@@ -266,14 +263,6 @@ __device__ __forceinline__ void ld_pair(uint32_t a, uint32_t b, float (&x)[16], 
         x[j] = __uint_as_float(rx[j]);
         y[j] = __uint_as_float(ry[j]);
     }
-}
-
-// A operand rows of both parts into one slot
-template <int MODE>
-__device__ __forceinline__ void put_group(unsigned char *slot, int t, const float (&vr)[16], const float (&vi)[16])
-{
-    put_row<MODE>(slot, t, vr);
-    put_row<MODE>(slot + 2 * TcLayout<MODE>::IMG_A, t, vi);
 }
 
 // lane j of a group: (degree n, order m), and whether it is used
@@ -356,12 +345,17 @@ __device__ __forceinline__ void ld_pair_n(uint32_t a, uint32_t b, float (&x)[LPT
     }
 }
 
-// Elements [LPT q, LPT q + LPT) of row t of the split A operand: pieces hi
-// and lo into the images at img and img + IMG_A.
+// Elements [LPT q, LPT q + LPT) of row t of the split A operand: the
+// pieces of v (+ lo, a float-float low word, or none) into the images at
+// img + i IMG_A.  Each piece is the input format's rounding of what the
+// earlier pieces left; the remainders are exact in FP32, so the pieces sum
+// to v + lo up to the last piece's rounding.
 template <int MODE, int LPT>
-__device__ __forceinline__ void put_part(unsigned char *img, int t, int q, const float (&v)[LPT])
+__device__ __forceinline__ void put_part(unsigned char *img, int t, int q, const float (&v)[LPT],
+                                         const float *lo = nullptr)
 {
     constexpr int IA = TcLayout<MODE>::IMG_A;
+    constexpr int NPC = TcFmt<MODE>::PIECES;
     unsigned char *row = img + (t >> 3) * TcFmt<MODE>::KC * 128 + (t & 7) * 16;
     if constexpr (MODE == 0) {  // 4 TF32 elements per core-matrix row
 #pragma unroll
@@ -377,25 +371,32 @@ __device__ __forceinline__ void put_part(unsigned char *img, int t, int q, const
             *reinterpret_cast<float4 *>(d + IA) = make_float4(l[0], l[1], l[2], l[3]);
         }
     } else {  // 8 BF16 elements per core-matrix row
-        uint32_t h[LPT / 2], l[LPT / 2];
+        uint32_t pc[NPC][LPT / 2];
 #pragma unroll
         for (int e = 0; e < LPT / 2; ++e) {
-            const float a = v[2 * e], b = v[2 * e + 1];
-            const __nv_bfloat162 hb = __floats2bfloat162_rn(a, b);
-            const __nv_bfloat162 lb = __floats2bfloat162_rn(a - __low2float(hb), b - __high2float(hb));
-            h[e] = *reinterpret_cast<const uint32_t *>(&hb);
-            l[e] = *reinterpret_cast<const uint32_t *>(&lb);
-        }
-        if constexpr (LPT == 4) {
-            unsigned char *d = row + (q >> 1) * 128 + (q & 1) * 8;
-            *reinterpret_cast<uint2 *>(d) = make_uint2(h[0], h[1]);
-            *reinterpret_cast<uint2 *>(d + IA) = make_uint2(l[0], l[1]);
-        } else {
+            float a = v[2 * e], b = v[2 * e + 1];
+            const float la = lo ? lo[2 * e] : 0.f, lb = lo ? lo[2 * e + 1] : 0.f;
 #pragma unroll
-            for (int c = 0; c < LPT / 8; ++c) {
-                unsigned char *d = row + ((LPT * q) / 8 + c) * 128;
-                *reinterpret_cast<uint4 *>(d) = make_uint4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
-                *reinterpret_cast<uint4 *>(d + IA) = make_uint4(l[4 * c], l[4 * c + 1], l[4 * c + 2], l[4 * c + 3]);
+            for (int k = 0; k < NPC; ++k) {
+                const __nv_bfloat162 hb = __floats2bfloat162_rn(a, b);
+                pc[k][e] = *reinterpret_cast<const uint32_t *>(&hb);
+                a -= __low2float(hb);  // exact
+                b -= __high2float(hb);
+                if (k == 0 && lo) {  // the low word joins the remainder (rounding ~2^-24 of it)
+                    a += la;
+                    b += lb;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NPC; ++k) {
+            if constexpr (LPT == 4) {
+                *reinterpret_cast<uint2 *>(row + (q >> 1) * 128 + (q & 1) * 8 + k * IA) = make_uint2(pc[k][0], pc[k][1]);
+            } else {
+#pragma unroll
+                for (int c = 0; c < LPT / 8; ++c)
+                    *reinterpret_cast<uint4 *>(row + ((LPT * q) / 8 + c) * 128 + k * IA) =
+                        make_uint4(pc[k][4 * c], pc[k][4 * c + 1], pc[k][4 * c + 2], pc[k][4 * c + 3]);
             }
         }
     }
@@ -423,9 +424,11 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
     using L = TcLayout<MODE>;
     using A = arith<ff>;
     constexpr int LPT = kTcNodes / NWG;
+    constexpr bool FF = TcFmt<MODE>::FF;
+    constexpr int kNE = kTcMaxOrder * (kTcMaxOrder + 1) / 2;  // stride of the edge tables' low words
     extern __shared__ __align__(1024) unsigned char smem[];
     const int P = p.P;
-    const TcSmem sm(P, L::IMG_A, L::IMG_B);
+    const TcSmem sm = TcSmem::of<MODE>(P);
     const int tid = threadIdx.x;
     const int t = tid & (kTcRows - 1);  // translation of the tile, tensor-memory lane
     const int q = tid >> 7;             // lanes [LPT q, LPT q + LPT) of every group
@@ -445,7 +448,7 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
 
     // constant operands (this order bound's groups) and edge factors, once per CTA
     {
-        const int nw = NG * 4 * L::IMG_B / 16, nh = NZ * 2 * L::IMG_B / 16;
+        const int nw = NG * L::GRP_W / 16, nh = NZ * L::GRP_H / 16;
         const uint4 *gw = reinterpret_cast<const uint4 *>(tt.W);
         const uint4 *gh = reinterpret_cast<const uint4 *>(tt.H);
         for (int i = tid; i < nw; i += kTcRows * NWG) reinterpret_cast<uint4 *>(smem + sm.w)[i] = gw[i];
@@ -453,6 +456,10 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
         for (int i = tid; i < P * (P + 1) / 2; i += kTcRows * NWG) {
             sEin[i] = tt.ein[i];
             sEout[i] = tt.eout[i];
+            if constexpr (FF) {  // low words at a fixed stride
+                sEin[kNE + i] = tt.ein[kNE + i];
+                sEout[kNE + i] = tt.eout[kNE + i];
+            }
         }
     }
     if (tid == 0) {
@@ -558,6 +565,12 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                     PW(3, m) = bs.hi;
                     RPW(0, m) = f.hi;
                     RPW(1, m) = g.hi;
+                    if constexpr (FF) {
+                        PW(4, m) = ac.lo;
+                        PW(5, m) = as.lo;
+                        RPW(2, m) = f.lo;
+                        RPW(3, m) = g.lo;
+                    }
                     if (m < max(pin, pout) && !(isfinite(f.hi) && isfinite(g.hi) && f.hi != 0.f && g.hi != 0.f))
                         range_ok = false;
                 }
@@ -611,23 +624,36 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
             const int sl = s & 1;
             if (s < NG) {  // group s: edge (r-power, e^{+i m alpha}, basis) -> A
                 const TcGroup gr = tc_deg_group(P, s);
-                float vr[LPT], vi[LPT];
+                float vr[LPT], vi[LPT], vr_lo[LPT], vi_lo[LPT];
 #pragma unroll
                 for (int jj = 0; jj < LPT; ++jj) {
                     const tcd::TcLane ln = tcd::deg_lane(gr, j0 + jj);
-                    vr[jj] = vi[jj] = 0.f;
+                    vr[jj] = vi[jj] = vr_lo[jj] = vi_lo[jj] = 0.f;
                     if (ln.on) {
-                        const float xr = tcd::f32_from_d(xr_n[jj]), xi = tcd::f32_from_d(xi_n[jj]);
-                        const float gg = RPW(0, ln.n) * sEin[ln.n * (ln.n + 1) / 2 + ln.m];
-                        const float gc = gg * PW(0, ln.m), gs = gg * PW(1, ln.m);
-                        vr[jj] = gc * xr - gs * xi;
-                        vi[jj] = gs * xr + gc * xi;
+                        const int e = ln.n * (ln.n + 1) / 2 + ln.m;
+                        if constexpr (FF) {  // float-float edge, split without rounding to FP32
+                            const ff xr = ff_from_d_int(xr_n[jj]), xi = ff_from_d_int(xi_n[jj]);
+                            const ff gg = A::mul(ff{RPW(0, ln.n), RPW(2, ln.n)}, ff{sEin[e], sEin[kNE + e]});
+                            const ff gc = A::mul(gg, ff{PW(0, ln.m), PW(4, ln.m)});
+                            const ff gs = A::mul(gg, ff{PW(1, ln.m), PW(5, ln.m)});
+                            const ff yr = A::dot2(gc, xr, A::neg(gs), xi), yi = A::dot2(gs, xr, gc, xi);
+                            vr[jj] = yr.hi;
+                            vr_lo[jj] = yr.lo;
+                            vi[jj] = yi.hi;
+                            vi_lo[jj] = yi.lo;
+                        } else {
+                            const float xr = tcd::f32_from_d(xr_n[jj]), xi = tcd::f32_from_d(xi_n[jj]);
+                            const float gg = RPW(0, ln.n) * sEin[e];
+                            const float gc = gg * PW(0, ln.m), gs = gg * PW(1, ln.m);
+                            vr[jj] = gc * xr - gs * xi;
+                            vi[jj] = gs * xr + gc * xi;
+                        }
                     }
                 }
                 if (s + 1 < NG) fetch(s + 1);
                 unsigned char *slot = sA + (s % 3) * L::SLOT;
-                tcd::put_part<MODE, LPT>(slot, t, q, vr);
-                tcd::put_part<MODE, LPT>(slot + 2 * L::IMG_A, t, q, vi);
+                tcd::put_part<MODE, LPT>(slot, t, q, vr, FF ? vr_lo : nullptr);
+                tcd::put_part<MODE, LPT>(slot + L::PART_A, t, q, vi, FF ? vi_lo : nullptr);
             }
             if (s >= 2) {  // group s-2: second swap -> state
                 sy.wait(1, sl);
@@ -659,17 +685,16 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                 }
                 unsigned char *slot = sA + ((s + 2) % 3) * L::SLOT;
                 tcd::put_part<MODE, LPT>(slot, t, q, vr);
-                tcd::put_part<MODE, LPT>(slot + 2 * L::IMG_A, t, q, vi);
+                tcd::put_part<MODE, LPT>(slot + L::PART_A, t, q, vi);
             }
             sy.step([&] {
                 if (s >= 1 && s <= NG) {
                     tcd::mma_group<MODE>(tbase + kTcD + 32 * (sl ^ 1), a0 + ((s + 2) % 3) * L::SLOT,
-                                         w0 + (s - 1) * 4 * L::IMG_B, 2 * L::IMG_B);
+                                         w0 + (s - 1) * L::GRP_W, L::PART_B);
                     sy.commit(1, sl ^ 1);
                 }
                 if (s < NG) {
-                    tcd::mma_group<MODE>(tbase + kTcD + 32 * sl, a0 + (s % 3) * L::SLOT, w0 + s * 4 * L::IMG_B,
-                                         2 * L::IMG_B);
+                    tcd::mma_group<MODE>(tbase + kTcD + 32 * sl, a0 + (s % 3) * L::SLOT, w0 + s * L::GRP_W, L::PART_B);
                     sy.commit(0, sl);
                 }
             });
@@ -691,7 +716,7 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                 }
                 unsigned char *slot = sA + (s % 3) * L::SLOT;
                 tcd::put_part<MODE, LPT>(slot, t, q, vr);
-                tcd::put_part<MODE, LPT>(slot + 2 * L::IMG_A, t, q, vi);
+                tcd::put_part<MODE, LPT>(slot + L::PART_A, t, q, vi);
             }
             if (s >= 1) {  // group s-1: output -> state
                 sy.wait(0, sl ^ 1);
@@ -721,7 +746,7 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
             }
             sy.step([&] {
                 if (s < NZ) {
-                    tcd::mma_group<MODE>(tbase + kTcD + 32 * sl, a0 + (s % 3) * L::SLOT, h0 + s * 2 * L::IMG_B, 0);
+                    tcd::mma_group<MODE>(tbase + kTcD + 32 * sl, a0 + (s % 3) * L::SLOT, h0 + s * L::GRP_H, 0);
                     sy.commit(0, sl);
                 }
             });
@@ -757,7 +782,7 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                 }
                 unsigned char *slot = sA + (s % 3) * L::SLOT;
                 tcd::put_part<MODE, LPT>(slot, t, q, vr);
-                tcd::put_part<MODE, LPT>(slot + 2 * L::IMG_A, t, q, vi);
+                tcd::put_part<MODE, LPT>(slot + L::PART_A, t, q, vi);
             }
             if (s >= 2) {  // group s-2: second swap -> e^{-i m alpha}, basis, r-power -> target +=
                 sy.wait(1, sl);
@@ -768,10 +793,22 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                 for (int jj = 0; jj < LPT; ++jj) {
                     const tcd::TcLane ln = tcd::deg_lane(gr, j0 + jj);
                     if (ln.on && ln.n < pout) {
-                        const float gg = RPW(1, ln.n) * sEout[ln.n * (ln.n + 1) / 2 + ln.m];
-                        const float gc = gg * PW(0, ln.m), gs = gg * PW(1, ln.m);
-                        const double orr = d_from_f_int(gc * ur[jj] + gs * ui[jj]);
-                        const double oi = d_from_f_int(gc * ui[jj] - gs * ur[jj]);
+                        const int e = ln.n * (ln.n + 1) / 2 + ln.m;
+                        double orr, oi;
+                        if constexpr (FF) {  // float-float edge
+                            const ff gg = A::mul(ff{RPW(1, ln.n), RPW(3, ln.n)}, ff{sEout[e], sEout[kNE + e]});
+                            const ff gc = A::mul(gg, ff{PW(0, ln.m), PW(4, ln.m)});
+                            const ff gs = A::mul(gg, ff{PW(1, ln.m), PW(5, ln.m)});
+                            const ff xr{ur[jj], 0.f}, xi{ui[jj], 0.f};
+                            const ff yr = A::dot2(gc, xr, gs, xi), yi = A::dot2(gc, xi, A::neg(gs), xr);
+                            orr = d_from_f_int(yr.hi) + d_from_f_int(yr.lo);
+                            oi = d_from_f_int(yi.hi) + d_from_f_int(yi.lo);
+                        } else {
+                            const float gg = RPW(1, ln.n) * sEout[e];
+                            const float gc = gg * PW(0, ln.m), gs = gg * PW(1, ln.m);
+                            orr = d_from_f_int(gc * ur[jj] + gs * ui[jj]);
+                            oi = d_from_f_int(gc * ui[jj] - gs * ur[jj]);
+                        }
                         double *pr = dp + ln.n * (ln.n + 1) + ln.m, *pi = dp + (ln.n + 1) * (ln.n + 1) + ln.m;
                         if (p.atomic) {
                             atomicAdd(pr, orr);
@@ -803,17 +840,16 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                 }
                 unsigned char *slot = sA + ((s + 2) % 3) * L::SLOT;
                 tcd::put_part<MODE, LPT>(slot, t, q, vr);
-                tcd::put_part<MODE, LPT>(slot + 2 * L::IMG_A, t, q, vi);
+                tcd::put_part<MODE, LPT>(slot + L::PART_A, t, q, vi);
             }
             sy.step([&] {
                 if (s >= 1 && s <= NG) {
                     tcd::mma_group<MODE>(tbase + kTcD + 32 * (sl ^ 1), a0 + ((s + 2) % 3) * L::SLOT,
-                                         w0 + (s - 1) * 4 * L::IMG_B, 2 * L::IMG_B);
+                                         w0 + (s - 1) * L::GRP_W, L::PART_B);
                     sy.commit(1, sl ^ 1);
                 }
                 if (s < NG) {
-                    tcd::mma_group<MODE>(tbase + kTcD + 32 * sl, a0 + (s % 3) * L::SLOT, w0 + s * 4 * L::IMG_B,
-                                         2 * L::IMG_B);
+                    tcd::mma_group<MODE>(tbase + kTcD + 32 * sl, a0 + (s % 3) * L::SLOT, w0 + s * L::GRP_W, L::PART_B);
                     sy.commit(0, sl);
                 }
             });

@@ -1,5 +1,5 @@
 """GPU tests of the tensor-core translation kernel (precision modes
-SFMM_TC_TF32 = 3 and SFMM_TC_BF16 = 4): the reference's golden outputs, the
+SFMM_TC_TF32 = 3, SFMM_TC_BF16 = 4, SFMM_TC_BF16X6 = 5): the reference's golden outputs, the
 FP64 naive oracle on mixed orders, repeated targets, permutations and index
 arrays, malformed entries, zero shifts, the host-memory calls, plans, and
 the routing of order bounds above 16 to the split kernel.
@@ -9,7 +9,10 @@ over the batch), from the operand precision of the split products:
   * 3xTF32 (two TF32 pieces, ~22 bits per operand, FP32 accumulation):
     4e-6 (measured up to 1.4e-6, L2L at P=16);
   * 3xBF16 (two BF16 pieces, ~16 bits per operand): 2e-4 (measured up to
-    6e-5, M2M at P=16).
+    6e-5, M2M at P=16);
+  * BF16x6 (three BF16 pieces, float-float edges): 1.5e-6 (measured up to
+    5e-7 on 1 000 translations, 6.2e-7 over 2e6 M2L at P=16: the FP32
+    accumulation in tensor memory rounds once per MMA stage).
 """
 import ctypes as C
 
@@ -20,8 +23,8 @@ from helpers import load_golden, norm_weights, per_degree_err, rel_err, rel_err_
 
 pytestmark = pytest.mark.gpu
 
-TC = {"tf32": 3, "bf16": 4}
-TOL = {3: 4e-6, 4: 2e-4}
+TC = {"tf32": 3, "bf16": 4, "bf16x6": 5}
+TOL = {3: 4e-6, 4: 2e-4, 5: 1.5e-6}
 CASES = load_golden()
 
 
