@@ -298,10 +298,92 @@ def cpu_leg(op, P, seconds_target, seed):
                       f"microkernels, {platform.machine()}, one worker per core)"}
 
 
+def run_c0(local, steps):
+    """M2L at P=10 over 100 000 translations (64 unit charges per source), plain
+    FP64 on the GPU, against the reference's own CPU translations on the same
+    inputs (its multithreaded_translator where the reference library was
+    built) and the FP64 naive oracle on the whole batch."""
+    import torch
+    import solidfmm_gb300 as sf
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle
+    from helpers import norm_weights, rel_err
+
+    dev = torch.device("cuda", local)
+    P, N = 10, 100_000
+    S = P * (P + 1)
+    ctx = sf.Context(P, "f64", device=local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    src, shift, pin = make_inputs(ctx, "m2l", P, N, 64, 77, dev)
+    dst = torch.zeros(N, S, dtype=torch.float64, device=dev)
+    ctx.translate_device("m2l", 0, N, src, S, N, dst, S, N, pin, pin, shift)
+    torch.cuda.synchronize()
+    got = dst.cpu().numpy()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.translate_device("m2l", 0, N, src, S, N, dst, S, N, pin, pin, shift)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    src_h, sh_h = src.cpu().numpy(), shift.cpu().numpy()
+    pin_h = np.full(N, P, np.uint32)
+    idx = np.arange(N, dtype=np.uint32)
+    ref = np.zeros((N, S))
+    pyoracle.naive("m2l", src_h, pin_h, ref, pin_h, sh_h)
+    w = norm_weights(P, "L")
+    row = {"workload": "M2L P=10, 100 000 translations, 64 unit charges per source, FP64",
+           "plain_fp64": {"value": N / (ms * 1e-3), "unit": "translations/s", "ms_per_step": ms},
+           "rel_err_vs_fp64_oracle": {"raw": rel_err(got, ref), "orthonormal": rel_err(got, ref, w)}}
+    native = not pyoracle.ref_available()  # the generic-dispatch checker where it was built, else native
+    if pyoracle.ref_available(native=native):
+        rd = np.zeros((N, S))
+        sec = pyoracle.reference("m2l", P, src_h, pin_h, rd, pin_h, sh_h, idx, idx, mode=3, native=native)
+        row["reference_cpu"] = {"value": N / sec, "unit": "translations/s", "cores": os.cpu_count(),
+                                "build": "native SIMD" if native else "generic microkernels"}
+        row["rel_err_vs_reference_double"] = {"raw": rel_err(got, rd), "orthonormal": rel_err(got, rd, w)}
+        row["reference_double_vs_oracle"] = {"raw": rel_err(rd, ref), "orthonormal": rel_err(rd, ref, w)}
+    return row
+
+
+def extras(args, local):
+    """Configurations beside the headline, in bounded time (tens of seconds):
+    config 0 (M2L P=10), config 1 (P=20 M2M/M2L/L2L, FP64 and FP32), config 3
+    (mixed orders, execution plan) and config 4 (FMM pass)."""
+    import torch
+
+    out = {}
+    t0 = time.perf_counter()
+    out["c0_m2l_p10"] = run_c0(local, max(3, args.steps // 4))
+    torch.cuda.empty_cache()
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = max(3, args.steps // 4)
+    sub.warmup = 2
+    r = run_ops20(sub, nested=True)
+    out["c1_p20"] = r["rows"] if r else None
+    torch.cuda.empty_cache()
+    r = run_mixed(sub, nested=True)
+    out["c3_mixed"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "plan", "plan_plain_fp64",
+                                         "unsorted_one_launch_per_op", "per_order_pair_launches", "config")} if r else None
+    torch.cuda.empty_cache()
+    r = run_fmm(sub, nested=True)
+    out["c4_fmm"] = {k: r[k] for k in ("value", "unit", "plain_fp64_ms_per_pass", "translations_per_s",
+                                       "leaf_local_rel_err_vs_oracle_pass",
+                                       "potential_rel_err_vs_direct_2000_particles", "cpu_baseline",
+                                       "config")} if r else None
+    torch.cuda.empty_cache()
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 MIXED_METRIC = "mixed M2L/M2M/L2L translations/s, orders U{4..24}, 1.5e6 per GPU"
 
 
-def run_mixed(args):
+def run_mixed(args, nested=False):
     """Mixed-order batch: 40% M2L, 30% M2M, 30% L2L with P_in, P_out iid
     U{4..24}, sources gathered from 65 536 P2M/P2L expansions per kind,
     distinct targets.  One execution plan (three stages, order-sorted
@@ -311,8 +393,9 @@ def run_mixed(args):
     import solidfmm_gb300 as sf
     from solidfmm_gb300 import build as _b
 
-    world, rank, local = dist_init(args)
-    _b.build()
+    world, rank, local = (1, 0, 0) if nested else dist_init(args)
+    if not nested:
+        _b.build()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     P, N = 24, WORKLOADS["mixed"][2]
@@ -431,13 +514,15 @@ def run_mixed(args):
             "per_order_pair_launches": {"split": rate(ms_pairs), "plain_fp64": rate(ms_pairs_plain),
                                         "launches_per_step": len(groups)},
             "clocks": clk, "gpu_launches": launches}
-    print(json.dumps(line))
+    if not nested:
+        print(json.dumps(line))
+    return line
 
 
 OPS_METRIC = "translations/s per operator and arithmetic, P=20, 1e6 translations"
 
 
-def run_ops20(args):
+def run_ops20(args, nested=False):
     """Every operator at P=20 in every arithmetic (1e6 translations, 128
     charges per source), with the relative error against the FP64 naive
     oracle on 500 translations; M2L at P=16 and P=17 beside it.  FP32 at
@@ -447,8 +532,9 @@ def run_ops20(args):
     import solidfmm_gb300 as sf
     from solidfmm_gb300 import build as _b
 
-    world, rank, local = dist_init(args)
-    _b.build()
+    world, rank, local = (1, 0, 0) if nested else dist_init(args)
+    if not nested:
+        _b.build()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -458,8 +544,10 @@ def run_ops20(args):
 
     pyoracle.build(with_ref=False)
     rows = []
-    for op, P, N in (("m2m", 20, 1_000_000), ("m2l", 20, 1_000_000), ("l2l", 20, 1_000_000),
-                     ("m2l", 16, 1_000_000), ("m2l", 17, 1_000_000)):
+    cases = [("m2m", 20, 1_000_000), ("m2l", 20, 1_000_000), ("l2l", 20, 1_000_000)]
+    if not nested:  # the other reading of "order P" beside the headline's
+        cases += [("m2l", 16, 1_000_000), ("m2l", 17, 1_000_000)]
+    for op, P, N in cases:
         S = P * (P + 1)
         ctx = sf.Context(P, "f64", device=local)
         ctx32 = sf.Context(P, "f32", device=local)
@@ -507,13 +595,15 @@ def run_ops20(args):
             "config": {"workload": "M2M/M2L/L2L at P=20 (1e6 each, 128 charges per source), M2L at P=16 and 17",
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
             "rows": rows}
-    print(json.dumps(line))
+    if not nested:
+        print(json.dumps(line))
+    return line
 
 
 FMM_METRIC = "FMM pass time (P2M + M2M + M2L + L2L), uniform octree depth 5, P=12, 32 charges per leaf"
 
 
-def run_fmm(args):
+def run_fmm(args, nested=False):
     """One FMM pass on a depth-5 uniform octree at P=12 (solidfmm_gb300.fmm):
     P2M at the leaves, M2M to level 2, M2L over the interaction lists of
     levels 2..5, L2L to the leaves, in one execution plan.  The leaf locals
@@ -525,8 +615,9 @@ def run_fmm(args):
     from solidfmm_gb300 import build as _b
     from solidfmm_gb300 import fmm
 
-    world, rank, local = dist_init(args)
-    _b.build()
+    world, rank, local = (1, 0, 0) if nested else dist_init(args)
+    if not nested:
+        _b.build()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     depth, P, per = 5, 12, 32
@@ -623,7 +714,9 @@ def run_fmm(args):
                              "sample": "the same pass (P2M + all translations) by the oracle's FP64 rotation-method "
                                        "port, one pthread per core"},
             "clocks": clk, "gpu_launches": launches}
-    print(json.dumps(line))
+    if not nested:
+        print(json.dumps(line))
+    return line
 
 
 def main():
@@ -635,6 +728,7 @@ def main():
     ap.add_argument("--workload", default="m2l16", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the other configurations")
     args = ap.parse_args()
     if args.workload == "mixed":
         return run_mixed(args)
@@ -892,6 +986,10 @@ def main():
             "roofline": roof, "issue_utilisation": issue_util, "roofline_compute": roof_compute,
             "roofline_plain_fp64": roof_fp64,
             "cpu_baseline": cpu, "cpu_baseline_port": cpu_port, "clocks": clk, "gpu_launches": launches}
+    if world == 1 and not args.no_extras and args.workload == "m2l16":
+        del src, dst, h_src, h_dst
+        torch.cuda.empty_cache()
+        line["configs"] = extras(args, local)
     print(json.dumps(line))
 
 
