@@ -197,6 +197,24 @@ int sfmm_tune(sfmm_context *ctx, int op, int precision, size_t order_bound, size
  * (order bound and size, all stages in order; returns their number). */
 typedef struct sfmm_plan sfmm_plan;
 int sfmm_plan_create(sfmm_context *ctx, sfmm_plan **plan);
+/* Plan options (before sfmm_plan_finalize; flags may be combined):
+ * SFMM_PLAN_FUSED  each stage runs as one persistent launch over all its
+ *                  orders: the grid fills the GPU once and its CTAs take
+ *                  tiles of the order-sorted stage from a device work list
+ *                  (largest orders first) until it is empty, with the launch
+ *                  shape of the stage's largest order bound.  Stages in a
+ *                  tensor-core precision keep one launch per segment.
+ * SFMM_PLAN_TUNE   finalize measures launch shapes and launches with the
+ *                  fastest: a fused stage's on a synthetic batch with the
+ *                  stage's own order distribution (a sample of up to 65 536
+ *                  of its translations; the shape stays with the plan), the
+ *                  segments' with sfmm_tune (uniform orders, min(max(count,
+ *                  4096), 65536) translations) for every (operator,
+ *                  precision, order bound) the context has not measured yet
+ *                  (the shape stays with the context).
+ * Default 0: one launch per segment, built-in shapes. */
+enum { SFMM_PLAN_FUSED = 1, SFMM_PLAN_TUNE = 2 };
+int sfmm_plan_set_options(sfmm_plan *plan, int options);
 int sfmm_plan_add(sfmm_plan *plan, int op, int precision, size_t n,
                   const void *src, size_t src_stride, size_t src_count, const uint32_t *src_index,
                   void *dst, size_t dst_stride, size_t dst_count, const uint32_t *dst_index,

@@ -17,6 +17,7 @@ F32, F64 = 0, 1
 M2M, M2L, L2L = 0, 1, 2
 PLAIN, SPLIT, SPLIT_FF, TC_TF32, TC_BF16, TC_BF16X6 = 0, 1, 2, 3, 4, 5
 TARGETS_UNIQUE, TARGETS_REPEAT = 0, 1
+PLAN_FUSED, PLAN_TUNE = 1, 2
 OPS = {"m2m": M2M, "m2l": M2L, "l2l": L2L}
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "ORDER_RANGE", 3: "OVERFLOW", 4: "DIM_MISMATCH", 5: "OOM",
@@ -29,7 +30,7 @@ EXPORTS = [
     "sfmm_host_table", "sfmm_measure_fma_peak", "sfmm_measure_imad_peak", "sfmm_bucket_by_order_noalloc",
     "sfmm_set_group", "sfmm_tune", "sfmm_plan_create", "sfmm_plan_add", "sfmm_plan_finalize", "sfmm_plan_run",
     "sfmm_plan_launches", "sfmm_plan_segments", "sfmm_plan_destroy", "sfmm_eval_device", "sfmm_bounding_sphere",
-    "sfmm_p2x_ragged_device",
+    "sfmm_p2x_ragged_device", "sfmm_plan_set_options",
 ]
 
 
@@ -90,6 +91,7 @@ def load():
     L.sfmm_plan_add.argtypes = [vp, C.c_int, C.c_int, sz, vp, sz, sz, u32p, vp, sz, sz, u32p, u32p, u32p, dp,
                                 C.c_int]
     L.sfmm_plan_finalize.argtypes = [vp]
+    L.sfmm_plan_set_options.argtypes = [vp, C.c_int]
     L.sfmm_plan_run.argtypes = [vp]
     L.sfmm_plan_launches.argtypes = [vp]
     L.sfmm_plan_launches.restype = sz
@@ -264,6 +266,13 @@ class Plan:
             self.h, OPS.get(op, op), precision, n, _ptr(src), src_stride, src_count, _ptr(src_index), _ptr(dst),
             dst_stride, dst_count, _ptr(dst_index), _ptr(p_in), _ptr(p_out), _ptr(shift),
             TARGETS_REPEAT if repeat else TARGETS_UNIQUE))
+        return self
+
+    def options(self, fused=False, tune=False):
+        """SFMM_PLAN_FUSED (one persistent launch per stage over a work list)
+        and SFMM_PLAN_TUNE (measured launch shapes), before finalize()."""
+        self.ctx._check(self.L.sfmm_plan_set_options(self.h, (PLAN_FUSED if fused else 0) |
+                                                     (PLAN_TUNE if tune else 0)))
         return self
 
     def finalize(self):

@@ -247,7 +247,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
               long long sstride, long long nsrc, const uint32_t *sidx, void *dst, long long dstride, long long ndst,
               const uint32_t *tidx, const uint32_t *pin, const uint32_t *pout, const double *shift,
               const uint32_t *perm, int flags, long long nidx, const unsigned long long *src_ptr,
-              const unsigned long long *dst_ptr, bool in_hbm)
+              const unsigned long long *dst_ptr, bool in_hbm, const WorkList *wl, const LaunchShape *shape)
 {
     if (n == 0) return SFMM_OK;
     static const char *const kName[3] = {"sfmm m2m launch", "sfmm m2l launch", "sfmm l2l launch"};
@@ -257,6 +257,7 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     LaunchShape s;
     int st = prepare_launch(c, op, a, Pbound, &s);
     if (st) return st;
+    if (shape && !is_tc(a)) s = *shape;
     KParams p{};
     p.op = op;
     p.P = Pbound;
@@ -280,6 +281,12 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.dst_ptr = dst_ptr;
     p.atomic = (flags & SFMM_TARGETS_REPEAT) ? 1 : 0;
     p.in_hbm = in_hbm ? 1 : 0;
+    if (wl) {
+        if (is_tc(a)) return fail(c, SFMM_UNSUPPORTED, "work lists run the split and plain kernels");
+        p.work = wl->work;
+        p.work_counter = wl->counter;
+        p.nwork = wl->n;
+    }
     if (is_tc(a)) {
         cudaError_t e = launch_translate_tc(p, c->tc[tc_mode(a)], c->num_sms, stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core translation kernel launch");
@@ -300,11 +307,19 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     p.H = t.H[op];
     p.spad = s.spad;
     p.TS = s.TS;
-    long long tiles = (n + s.TS - 1) / s.TS;
+    long long tiles = wl ? wl->n : (n + s.TS - 1) / s.TS;
     long long grid = (long long)c->num_sms * s.blocks_per_sm;
     if (grid > tiles) grid = tiles;
+    if (grid < 1) return fail(c, SFMM_CUDA_ERROR, "no launch shape runs order %d (G %d, %d translations per CTA)",
+                              Pbound, s.G, s.TS);
+    if (wl) {  // the tile descriptor's two words after the meta arrays
+        s.smem += 8;
+        if (s.smem > 232448) return fail(c, SFMM_UNSUPPORTED, "work-list launch above the shared-memory limit");
+    }
     cudaError_t e = launch_translate(a, p, s, (int)grid, stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "translation kernel launch");
+    if (e != cudaSuccess)
+        return fail(c, SFMM_CUDA_ERROR, "translation kernel launch (order %d, G %d, %d per CTA, %zu B shared, grid %lld): %s",
+                    Pbound, s.G, s.TS, s.smem, grid, cudaGetErrorString(e));
     c->launches++;
     return SFMM_OK;
 }
@@ -378,7 +393,7 @@ LaunchShape best_shape(Arith a, int P, int G, bool small_tiles, int min_threads)
             if (!s.acc) continue;
             s.blocks_per_sm = translate_blocks_per_sm(a, s);
             long th = (long)s.blocks_per_sm * s.threads;
-            if (th > best_threads || (small_tiles && th == best_threads)) {
+            if (th > 0 && (th > best_threads || (small_tiles && th == best_threads))) {
                 best_threads = th;
                 best = s;
             }
@@ -674,6 +689,10 @@ int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t
         return fail(c, SFMM_UNSUPPORTED, "no kernel for order %d", Pb);
     }
     set_shape(c, key, &best);
+    {
+        std::lock_guard<std::mutex> lk2(c->setup_mtx);
+        c->tuned.insert(std::make_tuple(op, (int)a, Pb));
+    }
     if (group) *group = best.G;
     if (rate) *rate = best_rate;
     return SFMM_OK;

@@ -11,6 +11,8 @@
 #include <cstdint>
 #include <map>
 #include <mutex>
+#include <set>
+#include <tuple>
 #include <string>
 #include <utility>
 #include <vector>
@@ -96,6 +98,7 @@ struct sfmm_context {
     int *d_woff8 = nullptr;                              // offsets of the 8-row padded swap blocks
     bool pageable_access = false;  // the GPU reads pageable host memory through the host page tables
     sfmm::SlotScratch slot_scratch;  // target table of the classic host call
+    std::set<std::tuple<int, int, int>> tuned;  // (op, arith, order bound) shapes measured by sfmm_tune
 };
 
 namespace sfmm {
@@ -116,6 +119,9 @@ int cuda_fail(sfmm_context *c, cudaError_t e, const char *what);
 int arith_of(sfmm_context *c, int precision, Arith *out);
 // upload the arithmetic's tables once
 int ensure_tables(sfmm_context *c, Arith a);
+// the arithmetic a batch of op with this order bound runs in (split M2M above
+// order 18 runs float-float; tensor-core modes above order 16 run split)
+Arith resolve_arith(Arith a, int op, int Pbound);
 // device address of a caller's host array when the kernels can use it
 // directly (pinned host memory, or pageable memory on a GPU that uses the host
 // page tables), else nullptr
@@ -125,11 +131,19 @@ const void *device_view(sfmm_context *c, const void *host);
 int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound, LaunchShape *shape = nullptr);
 // one validated translation launch on device pointers (translation i of the
 // batch is perm[i] when perm is given)
+// A work list (work, work_counter, nwork: see KParams) turns the launch into
+// one persistent grid that takes its tiles from the list; `shape` (may be
+// null) replaces the context's launch shape for this launch.
+struct WorkList {
+    const uint2 *work = nullptr;
+    unsigned *counter = nullptr;
+    long long n = 0;
+};
 int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound, long long n, const void *src,
               long long sstride, long long nsrc, const uint32_t *sidx, void *dst, long long dstride, long long ndst,
               const uint32_t *tidx, const uint32_t *pin, const uint32_t *pout, const double *shift,
               const uint32_t *perm, int flags, long long nidx = -1,
               const unsigned long long *src_ptr = nullptr, const unsigned long long *dst_ptr = nullptr,
-              bool in_hbm = true);
+              bool in_hbm = true, const WorkList *wl = nullptr, const LaunchShape *shape = nullptr);
 
 }  // namespace sfmm

@@ -20,21 +20,26 @@ template <class A, int G, int ACC, bool FIX>
 static cudaError_t launch_inst(const KParams &p, const LaunchShape &s, int grid, cudaStream_t st)
 {
     clear_stale_error();
-    if (p.in_hbm)
+    if (p.work) {
+        if (!p.in_hbm) return cudaErrorInvalidValue;  // work lists are a device-memory form
+        k_translate<A, G, ACC, FIX, true, true><<<grid, s.threads, s.smem, st>>>(p);
+    } else if (p.in_hbm) {
         k_translate<A, G, ACC, FIX, true><<<grid, s.threads, s.smem, st>>>(p);
-    else
+    } else {
         k_translate<A, G, ACC, FIX, false><<<grid, s.threads, s.smem, st>>>(p);
+    }
     return cudaGetLastError();
 }
 
 // resident CTAs per SM of the device-memory instance (the shape's grid
-// sizing); the host-memory instance uses no more resources
+// sizing); the host-memory and work-list instances are set up alongside
 template <class A, int G, int ACC, bool FIX>
 static int occupancy_inst(const LaunchShape &s)
 {
     auto kern = k_translate<A, G, ACC, FIX, true>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
     cudaFuncSetAttribute(k_translate<A, G, ACC, FIX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
+    cudaFuncSetAttribute(k_translate<A, G, ACC, FIX, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, s.threads, s.smem) != cudaSuccess) return 0;
     return nb;

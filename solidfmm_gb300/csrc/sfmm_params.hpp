@@ -3,6 +3,8 @@
 
 #include <cstdint>
 
+#include <vector_types.h>
+
 namespace sfmm {
 
 enum { OP_M2M = 0, OP_M2L = 1, OP_L2L = 2 };
@@ -45,6 +47,12 @@ struct KParams {
     // are then null and nsrc = ndst = nidx
     const unsigned long long *src_ptr;
     const unsigned long long *dst_ptr;
+    // work-list mode (non-null work): CTAs take tiles in the list's order from
+    // the counter (zero at launch); tile k covers entries [work[k].x,
+    // work[k].x + work[k].y) of the processing order, at most TS of them
+    const uint2 *work;
+    unsigned *work_counter;
+    long long nwork;
 };
 
 }  // namespace sfmm

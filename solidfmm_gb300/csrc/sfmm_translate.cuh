@@ -564,7 +564,9 @@ struct Geometry {
 // FIX selects block fixed-point swaps and beta rotations (float-float only).
 // HBM: expansions in device memory (L2 prefetch and a 4x unrolled gather);
 // false for host memory read over the link, where both cost end-to-end rate.
-template <class A, int G, int ACC, bool FIX = false, bool HBM = true>
+// WORK: tiles come from a work list (persistent launches of fused plans)
+// instead of a fixed stride over the batch.
+template <class A, int G, int ACC, bool FIX = false, bool HBM = true, bool WORK = false>
 __global__ void __launch_bounds__(256) k_translate(KParams p)
 {
     using AR = arith<A>;
@@ -602,9 +604,30 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
     Src *dst = reinterpret_cast<Src *>(p.dst);
     const int op = p.op;
 
-    for (long long tile = blockIdx.x; tile * TS < p.n; tile += gridDim.x) {
-        const long long i = tile * TS + slot;
+    for (long long tile = blockIdx.x;; tile += gridDim.x) {
+        // this tile's range of the processing order: a fixed stride over the
+        // batch, or the next entry of the work list (its two words after the
+        // meta arrays: work-list launches carry 8 more bytes of shared memory)
+        long long base = tile * TS;
+        int cnt = TS;
+        if constexpr (WORK) {
+            uint32_t *wsh = meta + 5 * TS;
+            if (tid == 0) {
+                const unsigned w = atomicAdd(p.work_counter, 1u);
+                const uint2 d = w < (unsigned long long)p.nwork ? p.work[w] : make_uint2(0u, 0xffffffffu);
+                wsh[0] = d.x;
+                wsh[1] = d.y;
+            }
+            __syncthreads();
+            if (wsh[1] == 0xffffffffu) break;
+            base = wsh[0];
+            cnt = (int)wsh[1];
+        } else if (base >= p.n) {
+            break;
+        }
+        const long long i = base + slot;
         bool valid = i < p.n;
+        if constexpr (WORK) valid = valid && slot < cnt;
         uint32_t t = 0, si = 0, ti = 0;
         if (valid) t = p.perm ? p.perm[i] : (uint32_t)i;
         int pin = 0, pout = 0;
@@ -679,7 +702,7 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         // end of the tile) and the next tile's sources (read at its start),
         // so that both phases meet L2 instead of DRAM.  Device arrays only;
         // every address lies inside an expansion the entry may touch.
-        if (HBM && !p.src_ptr) {
+        if (HBM && !WORK && !p.src_ptr) {
             const int tc = max(pout * (pout + 1), ident_p * (ident_p + 1));
             if (valid && tc) {
                 const char *dp = reinterpret_cast<const char *>(dst + (long long)ti * p.dstride);

@@ -177,3 +177,81 @@ def test_plan_finalize_retried_after_fixing_orders(native, oracle):
     torch.cuda.synchronize()
     ref = _oracle(oracle, "m2l", b)
     assert rel_err(d.cpu().numpy() - b["dst"], ref - b["dst"], norm_weights(P, "L")) < 1e-12
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["plain", "split", "split_ff"])
+@pytest.mark.parametrize("op", ["m2m", "m2l", "l2l"])
+def test_fused_plan_matches_segmented_plan(native, oracle, op, prec):
+    """SFMM_PLAN_FUSED: one persistent launch per stage over a work list of
+    order-sorted tiles gives the segmented plan's targets (and the oracle's),
+    replay after replay (the work counter is reset inside the graph)."""
+    import torch
+
+    ctx = native.Context(24, "f64")
+    b = _batch(op, (1, 24), (1, 24), 1500, 45)
+    ref = _oracle(oracle, op, b)
+    t = _dev(b)
+    S = b["src"].shape[1]
+    n = len(b["Pin"])
+    outs = {}
+    w = norm_weights(24, "M" if op == "m2m" else "L")
+    for fused in (False, True):
+        d = t["dst"].clone()
+        plan = native.Plan(ctx).add(op, prec, n, t["src"], S, n, d, S, n, t["Pin"], t["Pout"], t["xyz"],
+                                    src_index=t["sidx"], dst_index=t["tidx"]).options(fused=fused).finalize()
+        plan.run()
+        torch.cuda.synchronize()
+        outs[fused] = d.cpu().numpy()
+        if fused:
+            assert plan.launches == 1
+            plan.run()  # a second replay adds the same contribution again
+            torch.cuda.synchronize()
+            twice = d.cpu().numpy()
+            # raw coefficients span ~1e20: compare in the orthonormal basis
+            assert rel_err(twice - b["dst"], 2 * (outs[True] - b["dst"]), w) < 1e-12
+    assert ctx.device_status() == 0
+    tol = {0: 1e-12, 1: 1e-7, 2: 1e-11}[prec]
+    assert rel_err(outs[True] - b["dst"], ref - b["dst"], w) < tol
+    assert rel_err(outs[True] - b["dst"], outs[False] - b["dst"], w) < (2e-7 if prec == 1 else tol)
+
+
+def test_fused_tuned_plan_two_stages_repeat_targets(native, oracle):
+    """Fused and tuned together: two stages (M2M into shared parents with
+    atomics, then M2L), one launch each, with the launch shapes the tuner
+    measured at finalize."""
+    import torch
+
+    ctx = native.Context(12, "f64")
+    b1 = _batch("m2m", (2, 12), (2, 12), 600, 46, pattern="repeat")
+    b2 = _batch("m2l", (2, 12), (2, 12), 600, 47)
+    t1, t2 = _dev(b1), _dev(b2)
+    S = 12 * 13
+    n = 600
+    ref1 = _oracle(oracle, "m2m", b1)
+    d1 = t1["dst"].clone()
+    d2 = t2["dst"].clone()
+    plan = native.Plan(ctx)
+    plan.add("m2m", 0, n, t1["src"], S, n, d1, S, d1.shape[0], t1["Pin"], t1["Pout"], t1["xyz"],
+             src_index=t1["sidx"], dst_index=t1["tidx"], repeat=True)
+    plan.add("m2l", 0, n, t2["src"], S, n, d2, S, n, t2["Pin"], t2["Pout"], t2["xyz"],
+             src_index=t2["sidx"], dst_index=t2["tidx"])
+    plan.options(fused=True, tune=True).finalize()
+    plan.run()
+    torch.cuda.synchronize()
+    assert plan.launches == 2 and ctx.device_status() == 0
+    assert rel_err(d1.cpu().numpy() - b1["dst"], ref1 - b1["dst"]) < 1e-12
+    ref2 = _oracle(oracle, "m2l", b2)
+    assert rel_err(d2.cpu().numpy() - b2["dst"], ref2 - b2["dst"]) < 1e-12
+
+
+def test_plan_options_after_finalize_rejected(native):
+    import torch
+
+    ctx = native.Context(6, "f64")
+    b = _batch("m2l", 6, 6, 50, 48)
+    t = _dev(b)
+    plan = native.Plan(ctx).add("m2l", 0, 50, t["src"], 42, 50, t["dst"], 42, 50, t["Pin"], t["Pout"],
+                                t["xyz"]).finalize()
+    with pytest.raises(native.SfmmError):
+        plan.options(fused=True)
+    torch.cuda.synchronize()
