@@ -224,6 +224,41 @@ def accuracy(ctx, op, P, src, shift, pin, nsub, dev):
     return out
 
 
+def physics_table(ctx, P):
+    """The reference's own physics checks (tests/test_m2l.cpp:57-136,
+    test_m2m.cpp, test_l2l.cpp: a unit source expanded, translated 32 times
+    into one target, evaluated against 1/r and its gradient) for every
+    precision mode at order P, beside the same check with the oracle's exact
+    (naive O(P^4)) translation and with the reference's double and float."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle
+    from helpers import physics_errors, physics_gpu, physics_inputs, physics_reference
+
+    out = {}
+    for op in ("m2l", "m2m", "l2l"):
+        row = {}
+        E, shift = physics_inputs(op, P)
+        S = P * (P + 1)
+        exact = np.zeros((1, S))
+        pn = np.full(1, P, np.uint32)
+        pyoracle.naive(op, E.reshape(1, S), pn, exact, pn, shift.reshape(1, 3))
+        pe = physics_errors(op, P, exact[0])
+        row["oracle_exact_translation"] = {"potential": pe[0], "gradient": pe[1]}
+        for name, prec in (("plain_fp64", 0), ("split", 1), ("split_ff", 2), ("tc_tf32x3", 3), ("tc_bf16x3", 4),
+                           ("tc_bf16x6", 5)):
+            e = physics_gpu(ctx, op, P, prec)
+            row[name] = {"potential": e[0], "gradient": e[1]}
+        for nm, dt in (("reference_double", np.float64), ("reference_float", np.float32)):
+            if dt == np.float32 and P > 18:
+                continue
+            e = physics_reference(op, P, dt)
+            if e is not None:
+                row[nm] = {"potential": e[0], "gradient": e[1]}
+        out[op] = row
+    return out
+
+
 def workload_shifts(op, n, seed):
     """Shifts with the workload's geometry (numpy, seeded): M2L at distance
     U[2,4] in a uniform direction, M2M/L2L to a random octant corner."""
@@ -891,6 +926,7 @@ def main():
     classic_s = allmax(world, (time.perf_counter() - t0) / e2e_steps, dev)
 
     acc = accuracy(ctx, op, P, src, shift, pin, 1000, dev) if rank == 0 else None
+    physics = physics_table(ctx, P) if rank == 0 else None
 
     if rank != 0:
         return
@@ -977,6 +1013,11 @@ def main():
             "split_ff": {"value": ff_value, "ms_per_step": ms_ff,
                          "note": "float-float throughout (relative error ~1e-13)"},
             "accuracy_vs_fp64_oracle_1000": acc,
+            "physics_checks": {"what": "relative potential error r|phi - 1/r| and relative gradient error at the "
+                                       "reference's own test geometries (tests/test_{m2l,m2m,l2l}.cpp), order "
+                                       f"{P}, 32 translations into one target; the expansion's truncation error "
+                                       "is the oracle_exact_translation row",
+                               "rows": physics},
             "e2e": {"value": world * N / e2e_s, "unit": "translations/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "api": "sfmm_translate_host_packed on pinned host buffers: the kernel reads the sources and "

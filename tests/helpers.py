@@ -145,3 +145,80 @@ def rel_err_dev(got, ref, weights=None):
     den = ref.norm(dim=-1)
     ok = den > 0
     return float((num[ok] / den[ok]).max()) if bool(ok.any()) else float(num.max())
+
+
+# Fixed geometries of the reference's own physics checks (tests/test_m2l.cpp:
+# 57-60, test_m2m.cpp:55-58, test_l2l.cpp:54-57): unit source s, expansion
+# centres a (input) and b (output), evaluation point x.
+PHYSICS = {
+    "m2l": dict(s=(1.1, 0.2, 0.9), a=(1.0, 0.0, 1.0), b=(0.3, 0.1, 2.0), x=(0.1, 0.2, 2.5)),
+    "m2m": dict(s=(1.1, 0.2, 0.9), a=(1.0, 0.0, 1.0), b=(0.0, 0.0, 0.0), x=(3.1, 0.1, 2.5)),
+    "l2l": dict(s=(5.1, 0.2, 0.9), a=(1.0, 0.0, 1.0), b=(0.0, 0.0, 0.0), x=(0.1, 0.1, 0.2)),
+}
+
+
+def physics_inputs(op, P):
+    """Input expansion (R of the source about a for M2M/M2L, S for L2L, by the
+    oracle's harmonics) and the shift b - a of the reference's physics checks."""
+    import pyoracle
+
+    g = PHYSICS[op]
+    s, a, b = (np.asarray(g[k]) for k in ("s", "a", "b"))
+    d = s - a
+    E = pyoracle.harmonic("S" if op == "l2l" else "R", P, *d)
+    return E, b - a
+
+
+def physics_errors(op, P, out):
+    """Relative potential error r |phi - 1/r| and relative gradient error of
+    the translated expansion `out` (centred at b) at the evaluation point, as
+    the reference's tests print them; the gradient by central differences of
+    the oracle's harmonics (step 1e-4 of |x - b|, error ~1e-9 relative)."""
+    import pyoracle
+
+    g = PHYSICS[op]
+    s, b, x = (np.asarray(g[k]) for k in ("s", "b", "x"))
+    kind = "S" if op == "m2m" else "R"
+    r = float(np.linalg.norm(x - s))
+
+    def phi(p):
+        return pyoracle.dot(out, P, pyoracle.harmonic(kind, P, *(p - b)), P)
+
+    pot = phi(x)
+    h = 1e-4 * float(np.linalg.norm(x - b))
+    grad = np.array([(phi(x + h * e) - phi(x - h * e)) / (2 * h) for e in np.eye(3)])
+    exact = -(x - s) / r ** 3
+    return r * abs(pot - 1.0 / r), float(np.linalg.norm(grad - exact) / np.linalg.norm(exact))
+
+
+def physics_gpu(ctx, op, P, precision):
+    """The reference's physics check through the C ABI: 32 identical
+    translations into one target (accumulated with atomics), divided by 32."""
+    E, shift = physics_inputs(op, P)
+    S = P * (P + 1)
+    src = E.reshape(1, S)
+    dst = np.zeros((1, S))
+    n = 32
+    out = run_device(ctx, op, precision, src, dst, np.full(n, P, np.uint32), np.full(n, P, np.uint32),
+                     np.tile(shift, (n, 1)), sidx=np.zeros(n, np.uint32), tidx=np.zeros(n, np.uint32), repeat=True,
+                     order_bound=P)
+    return physics_errors(op, P, out[0] / n)
+
+
+def physics_reference(op, P, dtype=np.float64):
+    """The same check through the reference library (its classic single-thread
+    call, 32 translations into one target), or None where it was not built."""
+    import pyoracle
+
+    native = not pyoracle.ref_available()
+    if not pyoracle.ref_available(native=native):
+        return None
+    E, shift = physics_inputs(op, P)
+    S = P * (P + 1)
+    n = 32
+    src = E.reshape(1, S).astype(dtype)
+    dst = np.zeros((1, S), dtype)
+    pn = np.full(1, P, np.uint32)
+    pyoracle.reference(op, P, src, pn, dst, pn, np.tile(shift, (n, 1)).astype(dtype), np.zeros(n, np.uint32),
+                       np.zeros(n, np.uint32), mode=0, native=native)
+    return physics_errors(op, P, dst[0].astype(np.float64) / n)
