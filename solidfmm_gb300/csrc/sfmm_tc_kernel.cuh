@@ -520,19 +520,23 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
         const double *sp = p.src_ptr ? reinterpret_cast<const double *>(p.src_ptr[si]) : src + (long long)si * p.sstride;
         double *dp = p.dst_ptr ? reinterpret_cast<double *>(p.dst_ptr[ti]) : dst + (long long)ti * p.dstride;
 
-        // geometry (euler, microkernel_generic.cpp:37-97): the base values in
-        // FP64, their powers in float-float (this thread's orders m in
-        // [j0, j0 + LPT)), stored as FP32
+        // geometry (euler, microkernel_generic.cpp:37-97) and its powers in
+        // float-float (FP32 and integer pipes; the FP64 pipe runs at 1/64 of
+        // the FP32 rate), this thread's orders m in [j0, j0 + LPT), stored as FP32
         {
-            const double rxy = hypot(x, y);
-            const double rd = hypot(rxy, z), rinvd = 1.0 / rd;
-            double cad = 1, sad = 0;
-            if (rxy > 0) {
-                cad = y / rxy;
-                sad = x / rxy;
+            const ff fx = ff_from_d_int(x), fy = ff_from_d_int(y), fz = ff_from_d_int(z);
+            const ff rxy2 = A::dot2(fx, fx, fy, fy);
+            const ff rxy = ff_sqrt(rxy2);
+            const ff rr = ff_sqrt(A::add(rxy2, A::mul(fz, fz)));
+            const ff ri = ff_rcp(rr), one{1.f, 0.f}, zero{0.f, 0.f};
+            ff e1c = one, e1s = zero;
+            if (rxy.hi > 0.f) {
+                const ff rq = ff_rcp(rxy);
+                e1c = A::mul(fy, rq);
+                e1s = A::mul(fx, rq);
             }
-            ff eac = ff_from_d(cad), eas = ff_from_d(sad), ebc = ff_from_d(z * rinvd), ebs = ff_from_d(-rxy * rinvd);
-            const ff rr = ff_from_d(rd), ri = ff_from_d(rinvd), one{1.f, 0.f}, zero{0.f, 0.f};
+            const ff b1c = A::mul(fz, ri), b1s = A::neg(A::mul(rxy, ri));
+            ff eac = e1c, eas = e1s, ebc = b1c, ebs = b1s;
             // forward scale r^n (local input) or r^-(n+1) (multipole input);
             // backward r^(n+1) (multipole output) or r^-n (local output)
             ff f = op == OP_L2L ? one : ri, g = op == OP_M2M ? rr : one;
@@ -551,9 +555,7 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                 fs = A::mul(fs, fs);
                 gs = A::mul(gs, gs);
             }
-            // eac.. and fs.. now hold e^{i 2^k alpha} etc.; restart the single steps
-            const ff e1c = ff_from_d(cad), e1s = ff_from_d(sad), b1c = ff_from_d(z * rinvd),
-                     b1s = ff_from_d(-rxy * rinvd);
+            // eac.. and fs.. now hold e^{i 2^k alpha} etc.; the single steps
             const ff f1 = op == OP_L2L ? rr : ri, g1 = op == OP_M2M ? rr : ri;
 #pragma unroll
             for (int jj = 0; jj < LPT; ++jj) {
