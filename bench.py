@@ -162,7 +162,7 @@ def allmax(world, v, device):
 
 
 def make_inputs(ctx, op, P, N, nq, seed, dev):
-    """Sources by P2M/P2L on the GPU (FP64), shifts, orders."""
+    """Sources by P2M/P2L on the GPU (float-float), shifts, orders."""
     import torch
 
     g = torch.Generator(device=dev)

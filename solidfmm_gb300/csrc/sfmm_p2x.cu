@@ -4,7 +4,8 @@
 // fmadd(q, harmonics::R/S(P, x - c), E) (solid.cpp:70-104) with the R and S
 // recurrences of harmonics.cpp:32-80 and :177-224, evaluated column by column
 // (fixed m, increasing n) so that each coefficient is accumulated as soon as
-// it is produced.  One thread per expansion, FP64 arithmetic.
+// it is produced.  Orders up to 24: float-float arithmetic on the FP32 pipe,
+// lanes owning column pairs (k_p2x_ff); above, one FP64 thread per expansion.
 //
 // Bucketing: a counting sort of translation indices by the key
 // (p_in, p_out), so that warps see uniform orders.
@@ -14,6 +15,7 @@
 #include <mutex>
 
 #include "sfmm.h"
+#include "sfmm_arith.cuh"
 #include "sfmm_launch.hpp"
 
 namespace sfmm {
@@ -108,11 +110,335 @@ __global__ void k_p2x(int kind, int P, long long nexp, long long nq, const uint3
     }
 }
 
+// ---- float-float P2M / P2L for order bounds up to 24 ----
+//
+// The same sums on the FP32 pipe.  Coordinates are scaled by a power of two
+// rho per expansion (x' = (x - c) / rho, |x'| <= 1 for P2M from the farthest
+// charge, |x'| >= 1 for P2L from the nearest) and the columns run on the
+// Schmidt-normalised harmonics
+//     T_n^m = R_n^m(x') sig(n,m),  U_n^m = S_n^m(x') / sig(n,m),
+//     sig(n,m) = sqrt((n+m)! (n-m)!),
+// which are bounded by |x'|^n and |x'|^-(n+1), so that no intermediate leaves
+// the FP32 range at any order here.  Both obey one recurrence,
+//     X_m^m     = d_m v X_{m-1}^{m-1},  d_m = sqrt((2m-1)/(2m)),
+//     X_n^m     = a(n,m) zeta X_{n-1}^m - b(n,m) eta X_{n-2}^m,
+//     a(n,m)    = (2n-1) / sqrt((n+m)(n-m)),
+//     b(n,m)    = sqrt((n+m-1)(n-m-1) / ((n+m)(n-m))),
+// with v = x'+iy', zeta = z', eta = |x'|^2 for T (X_0^0 = 1) and
+// v = (x'+iy')/|x'|^2, zeta = z'/|x'|^2, eta = 1/|x'|^2 for U (X_0^0 = 1/|x'|):
+// harmonics.cpp:32-80 (R) and :177-224 (S) with the normalisation folded into
+// the coefficients.  The sums come back to the reference's harmonics once per
+// expansion, in FP64: R_n^m(x) = rho^n T / sig, S_n^m(x) = sig U / rho^(n+1).
+//
+// LP lanes per expansion (LP a power of two, LP <= P <= 2 LP): lane l owns
+// columns m1 = l and m2 = P-1-l (one column when they coincide, none when
+// m1 > m2), P + 1 harmonics at most per lane.  A chunk of LP charges is
+// prepared one per lane (shift, scale, conversion to float-float) and
+// broadcast by shuffles; the diagonals v^m come from a prefix product across
+// the lanes; the harmonics accumulate in registers and are added to the
+// expansion once.
+constexpr int kP2xColsMax = 24;
+
+// Tables, evaluated at compile time in FP64: coefficient pairs [s][m] for
+// n = m + s as (a.hi, a.lo, b.hi, b.lo), the diagonal constants
+// d_1 ... d_m as float-float, sig(n, m) and 1/sig(n, m) at n(n+1)/2 + m.
+struct P2xTables {
+    float4 ab[kP2xColsMax][kP2xColsMax];
+    float2 diag[kP2xColsMax];
+    double sig[kP2xColsMax * (kP2xColsMax + 1) / 2];
+    double isig[kP2xColsMax * (kP2xColsMax + 1) / 2];
+};
+
+namespace p2x_tables {
+constexpr double csqrt(double x)
+{
+    if (!(x > 0)) return 0.0;
+    double f = 1.0;
+    while (x > 4.0) {  // exact rescaling into [1/4, 4]
+        x *= 0.25;
+        f *= 2.0;
+    }
+    while (x < 0.25) {
+        x *= 4.0;
+        f *= 0.5;
+    }
+    double r = 1.0;
+    for (int i = 0; i < 12; ++i) r = 0.5 * (r + x / r);
+    return r * f;
+}
+constexpr float2 split(double v)
+{
+    const float h = (float)v;
+    return float2{h, (float)(v - (double)h)};
+}
+constexpr double fact(int k)
+{
+    double f = 1.0;
+    for (int i = 2; i <= k; ++i) f *= i;
+    return f;
+}
+constexpr P2xTables make()
+{
+    P2xTables t{};
+    double dm = 1.0;  // product of (2i-1)/(2i), i <= m
+    for (int m = 0; m < kP2xColsMax; ++m) {
+        if (m > 0) dm *= (double)(2 * m - 1) / (double)(2 * m);
+        t.diag[m] = split(csqrt(dm));
+        for (int n = m; n < kP2xColsMax; ++n) {
+            const int s = n - m;
+            if (s >= 1) {
+                const double nm = (double)(n + m) * (double)(n - m);
+                const float2 a = split((double)(2 * n - 1) / csqrt(nm));
+                const float2 b = split(csqrt((double)(n + m - 1) * (double)(n - m - 1) / nm));
+                t.ab[s][m] = float4{a.x, a.y, b.x, b.y};
+            }
+            const double sg = csqrt(fact(n + m) * fact(n - m));
+            t.sig[n * (n + 1) / 2 + m] = sg;
+            t.isig[n * (n + 1) / 2 + m] = 1.0 / sg;
+        }
+    }
+    return t;
+}
+}  // namespace p2x_tables
+
+__device__ const P2xTables kP2xTab = p2x_tables::make();
+
+struct cff {
+    ff r, i;
+};
+__device__ __forceinline__ ff ff_shfl(ff a, int src, int width)
+{
+    return ff{__shfl_sync(0xffffffffu, a.hi, src, width), __shfl_sync(0xffffffffu, a.lo, src, width)};
+}
+__device__ __forceinline__ cff cff_shfl(cff a, int src, int width)
+{
+    return cff{ff_shfl(a.r, src, width), ff_shfl(a.i, src, width)};
+}
+
+// a x - b y with one renormalisation (19 FP32 operations)
+__device__ __forceinline__ ff ff_fms2(ff a, ff x, ff b, ff y)
+{
+    const float p = __fmul_rn(a.hi, x.hi);
+    float e = __fmaf_rn(a.hi, x.hi, -p);
+    e = __fmaf_rn(a.hi, x.lo, e);
+    e = __fmaf_rn(a.lo, x.hi, e);
+    const float q = __fmul_rn(b.hi, y.hi);
+    float f = __fmaf_rn(b.hi, y.hi, -q);
+    f = __fmaf_rn(b.hi, y.lo, f);
+    f = __fmaf_rn(b.lo, y.hi, f);
+    // TwoSum(p, -q)
+    const float s = __fsub_rn(p, q);
+    const float v = __fsub_rn(s, p);
+    const float t = __fsub_rn(__fsub_rn(p, __fsub_rn(s, v)), __fadd_rn(q, v));
+    return ff_norm(s, __fadd_rn(t, __fsub_rn(e, f)));
+}
+
+__device__ __forceinline__ cff cff_mul(cff a, cff b)
+{
+    return cff{ff_fms2(a.r, b.r, a.i, b.i), ff_fms2(a.r, b.i, ff{-a.i.hi, -a.i.lo}, b.r)};
+}
+
+// acc += x, the rounding error of the high words kept in the low word
+__device__ __forceinline__ void ffacc_add(ffacc &a, ff x)
+{
+    const float s = __fadd_rn(a.hi, x.hi);
+    const float v = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(x.hi, v));
+    a.hi = s;
+    a.lo = __fadd_rn(a.lo, __fadd_rn(e, x.lo));
+}
+
+// x 2^sh as float-float, integer and FP32 operations only (ff_from_d_int with
+// the shift folded into the exponent); |x 2^sh| < 2^-151 becomes 0.
+__device__ __forceinline__ ff ff_from_d_scaled(double x, int sh)
+{
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    const unsigned A = 0x800000u | ((hw & 0xfffffu) << 3) | (lw >> 29);
+    const unsigned B = lw & 0x1fffffffu;
+    const int k = min(e - 1023 - 23 + sh, 106);
+    float h = ldexp2(__uint2float_rn(A), k);
+    float l = ldexp2(__uint2float_rn(B), k - 29);
+    if (e == 0 || e - 1023 + sh < -151) h = l = 0.f;
+    if (hw >> 31) {
+        h = -h;
+        l = -l;
+    }
+    return ff_norm(h, l);
+}
+
+// A lane's two columns as one run of P + 1 harmonics: column m1 at t < len1
+// (t = n - m1), then column m2 at t = len1 + n - m2.  X starts at each
+// diagonal (dg1, dg2) and follows the recurrence, each value added to acc[t].
+// ab: this block's coefficient table.
+template <int NT>
+__device__ __forceinline__ void p2x_columns_ff(const float4 *ab, int m1, int len1, int m2, int tot, cff dg1,
+                                               cff dg2, ff zeta, ff eta, ffacc (&ar)[NT], ffacc (&ai)[NT])
+{
+    cff x1 = dg1, x2 = cff{ff{0.f, 0.f}, ff{0.f, 0.f}};
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        if (t >= tot) break;
+        if (t > 0) {
+            const bool second = t >= len1;
+            const int m = second ? m2 : m1, s = second ? t - len1 : t;
+            const float4 c = ab[(s > 0 ? s : 1) * kP2xColsMax + m];
+            const ff A = ff_mul(ff{c.x, c.y}, zeta), B = ff_mul(ff{c.z, c.w}, eta);
+            cff x = cff{ff_fms2(A, x1.r, B, x2.r), ff_fms2(A, x1.i, B, x2.i)};
+            if (s == 0) {  // the second column's diagonal
+                x = dg2;
+                x1 = cff{ff{0.f, 0.f}, ff{0.f, 0.f}};
+            }
+            x2 = x1;
+            x1 = x;
+        }
+        ffacc_add(ar[t], x1.r);
+        ffacc_add(ai[t], x1.i);
+    }
+}
+
+template <class Out>
+__device__ __forceinline__ void p2x_put(Out *o, int kind, int sh, int n, int m, ffacc re, ffacc im)
+{
+    const int t = n * (n + 1) / 2 + m;
+    const double f = kind == 0 ? ldexp(kP2xTab.isig[t], sh * n) : ldexp(kP2xTab.sig[t], -sh * (n + 1));
+    o[n * (n + 1) + m] += (Out)(((double)re.hi + (double)re.lo) * f);
+    o[(n + 1) * (n + 1) + m] += (Out)(((double)im.hi + (double)im.lo) * f);
+}
+
+template <class Out, int LP>
+__global__ void __launch_bounds__(128) k_p2x_ff(int kind, int P, long long nexp, long long nq,
+                                                const uint32_t *__restrict__ offset, const double *__restrict__ q,
+                                                const double *__restrict__ pos, const double *__restrict__ centre,
+                                                Out *out, long long stride)
+{
+    // P + 1 <= 2 LP + 1 harmonics per lane
+    constexpr int NT = (2 * LP < kP2xColsMax ? 2 * LP : kP2xColsMax) + 1;
+    __shared__ float4 ab[kP2xColsMax * kP2xColsMax];
+    for (int i = threadIdx.x; i < P * kP2xColsMax; i += blockDim.x) ab[i] = (&kP2xTab.ab[0][0])[i];
+    __syncthreads();
+
+    const int l = threadIdx.x % LP;
+    const long long j = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / LP;
+    const bool live = j < nexp;
+    const int m1 = l, m2 = P - 1 - l;  // 0 <= m2 < P
+    const int len1 = (live && m1 <= m2) ? P - m1 : 0;
+    const int tot = len1 + ((live && m1 < m2) ? P - m2 : 0);
+    long long kb = 0, cnt = 0;
+    double cx = 0, cy = 0, cz = 0;
+    if (live) {
+        kb = offset ? (long long)offset[j] : j * nq;
+        cnt = (offset ? (long long)offset[j + 1] : (j + 1) * nq) - kb;
+        cx = centre[3 * j];
+        cy = centre[3 * j + 1];
+        cz = centre[3 * j + 2];
+    }
+    // rho = 2^sc: the largest (P2M) or smallest (P2L) distance of the
+    // expansion's charges rounded to a power of two, up (P2M) or down (P2L)
+    float ext = kind == 0 ? 0.f : __int_as_float(0x7f800000);
+    for (long long it = l; it < cnt; it += LP) {
+        const double *pp = pos + 3 * (kb + it);
+        const float dx = (float)(pp[0] - cx), dy = (float)(pp[1] - cy), dz = (float)(pp[2] - cz);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        ext = kind == 0 ? fmaxf(ext, r2) : fminf(ext, r2);
+    }
+    for (int d = LP / 2; d > 0; d >>= 1) {
+        const float o = __shfl_xor_sync(0xffffffffu, ext, d, LP);
+        ext = kind == 0 ? fmaxf(ext, o) : fminf(ext, o);
+    }
+    int sh = 0;  // log2 rho
+    if (ext > 0.f && ext < __int_as_float(0x7f800000)) {
+        int E;
+        frexpf(ext, &E);  // ext = f 2^E, f in [1/2, 1)
+        sh = kind == 0 ? (E + 1) >> 1 : (E - 1) >> 1;  // rho^2 >= ext (P2M), rho^2 <= ext / 2 (P2L)
+        sh = max(-100, min(100, sh));
+    }
+
+    ffacc ar[NT], ai[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) ar[t] = ai[t] = ffacc{0.f, 0.f};
+    const ff d1 = ff{kP2xTab.diag[m1].x, kP2xTab.diag[m1].y}, d2 = ff{kP2xTab.diag[m2].x, kP2xTab.diag[m2].y};
+    const int e = P - LP;  // 0 <= e <= LP
+
+    // chunk loop bound uniform over the warp (the shuffles need every lane)
+    const unsigned cntw = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
+    for (unsigned c0 = 0; c0 < cntw; c0 += LP) {
+        // this lane's charge of the chunk
+        ff zeta{0.f, 0.f}, eta{0.f, 0.f}, w{0.f, 0.f};
+        cff v{ff{0.f, 0.f}, ff{0.f, 0.f}};
+        if (c0 + l < cnt) {
+            const long long k = kb + c0 + l;
+            const double *pp = pos + 3 * k;
+            const ff x = ff_from_d_scaled(pp[0] - cx, -sh), y = ff_from_d_scaled(pp[1] - cy, -sh),
+                     z = ff_from_d_scaled(pp[2] - cz, -sh);
+            const ff r2 = ff_add(ff_add(ff_mul(x, x), ff_mul(y, y)), ff_mul(z, z));
+            w = ff_from_d_int(q[k]);
+            if (kind == 0) {
+                zeta = z;
+                eta = r2;
+                v = cff{x, y};
+            } else {
+                const ff ri = ff_rcp(r2);
+                zeta = ff_mul(z, ri);
+                eta = ri;
+                v = cff{ff_mul(x, ri), ff_mul(y, ri)};
+                w = ff_mul(w, ff_sqrt(ri));  // U_0^0 = 1/|x'|
+            }
+        }
+        for (int i = 0; i < LP; ++i) {
+            const ff zi = ff_shfl(zeta, i, LP), ei = ff_shfl(eta, i, LP), wi = ff_shfl(w, i, LP);
+            const cff vi = cff_shfl(v, i, LP);
+            // v^l by a prefix product over the lanes; v^m2 = v^(P-LP) v^(LP-1-l)
+            cff pw = l == 0 ? cff{ff{1.f, 0.f}, ff{0.f, 0.f}} : vi;
+#pragma unroll
+            for (int d = 1; d < LP; d <<= 1) {
+                const cff o = cff_shfl(pw, l >= d ? l - d : l, LP);
+                if (l >= d) pw = cff_mul(pw, o);
+            }
+            cff ue = cff_shfl(pw, e < LP ? e : LP - 1, LP);
+            if (e == LP) ue = cff_mul(ue, vi);
+            const cff pm2 = cff_mul(ue, cff_shfl(pw, LP - 1 - l, LP));
+            const ff k1 = ff_mul(d1, wi), k2 = ff_mul(d2, wi);
+            p2x_columns_ff<NT>(ab, m1, len1, m2, tot, cff{ff_mul(pw.r, k1), ff_mul(pw.i, k1)},
+                               cff{ff_mul(pm2.r, k2), ff_mul(pm2.i, k2)}, zi, ei, ar, ai);
+        }
+    }
+    if (!tot) return;
+    // back to R_n^m(x) = rho^n T / sig (P2M) or S_n^m(x) = sig U / rho^(n+1) (P2L)
+    Out *o = out + j * stride;
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+        if (t < tot) {
+            if (t < len1) p2x_put(o, kind, sh, m1 + t, m1, ar[t], ai[t]);
+            else p2x_put(o, kind, sh, m2 + t - len1, m2, ar[t], ai[t]);
+        }
+}
+
 cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const uint32_t *offset,
                        const double *q, const double *pos, const double *centre, void *out, long long stride,
                        cudaStream_t st)
 {
     if (nexp == 0) return cudaSuccess;
+    if (P <= kP2xColsMax) {  // lanes per expansion: LP <= P <= 2 LP
+        const int LP = P <= 2 ? (P == 1 ? 1 : 2) : P <= 4 ? 2 : P <= 8 ? 4 : P <= 16 ? 8 : 16;
+        const int tb = 128;
+        const long long grid = (nexp * LP + tb - 1) / tb;
+        clear_stale_error();
+#define SFMM_P2X_FF(T, L) k_p2x_ff<T, L><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, offset, q, pos, centre, \
+                                                                      (T *)out, stride)
+#define SFMM_P2X_LP(T)              \
+    switch (LP) {                   \
+    case 1: SFMM_P2X_FF(T, 1); break;  \
+    case 2: SFMM_P2X_FF(T, 2); break;  \
+    case 4: SFMM_P2X_FF(T, 4); break;  \
+    case 8: SFMM_P2X_FF(T, 8); break;  \
+    default: SFMM_P2X_FF(T, 16); break; \
+    }
+        if (f64) SFMM_P2X_LP(double) else SFMM_P2X_LP(float)
+#undef SFMM_P2X_LP
+#undef SFMM_P2X_FF
+        return cudaGetLastError();
+    }
     int tb = 128;
     long long grid = (nexp + tb - 1) / tb;
     clear_stale_error();

@@ -35,6 +35,31 @@ def norm_weights(P: int, kind: str) -> np.ndarray:
     return w
 
 
+def p2x_abs_scale(P, kind, q, pos, cen):
+    """Per coefficient of a P2M (kind 0) or P2L (kind 1) sum, the sum of the
+    absolute values of its terms' bounds: sum_k |q_k| |x_k|^n / sig(n,m) for R
+    and sum_k |q_k| sig(n,m) / |x_k|^(n+1) for S, sig(n,m) = sqrt((n+m)!(n-m)!)
+    (|R_n^m| and |S_n^m| never exceed those).  Rounding errors of the sum
+    scale with it, not with the sum itself, which may cancel."""
+    d = np.asarray(pos, np.float64) - np.asarray(cen, np.float64)[:, None, :]
+    r = np.linalg.norm(d, axis=2)
+    aq = np.abs(np.asarray(q, np.float64))
+    out = np.zeros((aq.shape[0], S_of(P)))
+    for n in range(P):
+        s = (aq * (r ** n if kind == 0 else r ** (-(n + 1)))).sum(1)
+        for m in range(n + 1):
+            sg = math.sqrt(math.factorial(n + m) * math.factorial(n - m))
+            out[:, n * (n + 1) + m] = out[:, (n + 1) * (n + 1) + m] = s / sg if kind == 0 else s * sg
+    return out
+
+
+def p2x_err(got, ref, P, kind, q, pos, cen):
+    """max over coefficients of |got - ref| / p2x_abs_scale."""
+    sc = p2x_abs_scale(P, kind, q, pos, cen)
+    err = np.abs(np.asarray(got, np.float64) - np.asarray(ref, np.float64))
+    return float(np.max(np.where(sc > 0, err / np.where(sc > 0, sc, 1.0), err)))
+
+
 def rel_err(got, ref, weights=None):
     """max over rows of the relative L2 error (optionally weighted)."""
     got = np.asarray(got, np.float64)
