@@ -402,8 +402,9 @@ def extras(args, local):
     out["c1_p20"] = r["rows"] if r else None
     torch.cuda.empty_cache()
     r = run_mixed(sub, nested=True)
-    out["c3_mixed"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "plan", "plan_segmented",
-                                         "unsorted_one_launch_per_op", "per_order_pair_launches", "config")} if r else None
+    keys = ("value", "unit", "ms_per_step", "value_from", "plan_fused", "plan_segmented", "unsorted_one_launch_per_op",
+            "per_order_pair_launches", "config")
+    out["c3_mixed"] = {k: r[k] for k in keys} if r else None
     torch.cuda.empty_cache()
     r = run_fmm(sub, nested=True)
     out["c4_fmm"] = {k: r[k] for k in ("value", "unit", "plain_fp64_ms_per_pass", "translations_per_s",
@@ -490,11 +491,11 @@ def run_mixed(args, nested=False):
     # the configuration's own form: one persistent fused launch per operator,
     # launch shapes measured by the tuner, captured in a CUDA graph
     plan_ft = plan_for(1, fused=True, tune=True)
+    plan_split = plan_for(1)  # one launch per order segment, segments on four concurrent graph branches
     clocks.start()
     ms_ft, launches = timed(plan_ft.run, args.steps, args.warmup)
+    ms_plan, seg_launches = timed(plan_split.run, args.steps, args.warmup)
     clk = clocks.stop()
-    plan_split = plan_for(1)  # one launch per order segment (shapes now tuned where measured)
-    ms_plan, seg_launches = timed(plan_split.run, max(2, args.steps // 2), 1)
     plan_fused_plain = plan_for(0, fused=True, tune=True)
     ms_ft_plain, _ = timed(plan_fused_plain.run, max(2, args.steps // 2), 1)
     plan_plain = plan_for(0)
@@ -540,8 +541,11 @@ def run_mixed(args, nested=False):
         return
     segs = plan_split.segments()
     rate = lambda ms: world * N / (ms * 1e-3)  # noqa: E731
-    line = {"metric": MIXED_METRIC, "value": rate(ms_ft), "unit": "translations/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_ft, "higher_is_better": True,
+    # the value is the faster plan form; both are reported
+    fused_wins = ms_ft <= ms_plan
+    ms_best = ms_ft if fused_wins else ms_plan
+    line = {"metric": MIXED_METRIC, "value": rate(ms_best), "unit": "translations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_best, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "split (int32 block fixed point rotations, float-float z-translation, f64 accumulation)",
             "data": "synthetic (seeded P2M/P2L sources, random orders and shifts)",
@@ -549,15 +553,19 @@ def run_mixed(args, nested=False):
                                    "gathered from 65 536 expansions per kind, distinct targets, FP64 storage at "
                                    "stride 600", "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}"},
-            "plan": {"form": "fused: one persistent launch per operator over a device work list of "
-                             "order-sorted tiles, launch shapes measured by sfmm_tune at finalize",
-                     "launches_per_step": launches, "cuda_graph": True, "plain_fp64": rate(ms_ft_plain)},
-            "plan_segmented": {"split": rate(ms_plan), "plain_fp64": rate(ms_plan_plain), "segments": len(segs),
-                               "launches_per_step": seg_launches},
+            "value_from": "plan_fused" if fused_wins else "plan_segmented",
+            "plan_fused": {"form": "one persistent launch per operator over a device work list of order-sorted "
+                                   "tiles, launch shapes measured by sfmm_tune at finalize (SFMM_PLAN_FUSED | "
+                                   "SFMM_PLAN_TUNE)", "split": rate(ms_ft), "plain_fp64": rate(ms_ft_plain),
+                           "launches_per_step": launches, "cuda_graph": True},
+            "plan_segmented": {"form": "one launch per order-bound segment at that order's own launch shape, the "
+                                       "segments of an operator on four concurrent graph branches (the default)",
+                               "split": rate(ms_plan), "plain_fp64": rate(ms_plan_plain), "segments": len(segs),
+                               "launches_per_step": seg_launches, "cuda_graph": True},
             "unsorted_one_launch_per_op": {"split": rate(ms_unsorted), "plain_fp64": rate(ms_unsorted_plain)},
             "per_order_pair_launches": {"split": rate(ms_pairs), "plain_fp64": rate(ms_pairs_plain),
                                         "launches_per_step": len(groups)},
-            "clocks": clk, "gpu_launches": launches}
+            "clocks": clk, "gpu_launches": launches if fused_wins else seg_launches}
     if not nested:
         print(json.dumps(line))
     return line

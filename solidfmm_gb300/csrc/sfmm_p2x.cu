@@ -203,16 +203,16 @@ constexpr P2xTables make()
 
 __device__ const P2xTables kP2xTab = p2x_tables::make();
 
-struct cff {
+struct cpx_ff {
     ff r, i;
 };
 __device__ __forceinline__ ff ff_shfl(ff a, int src, int width)
 {
     return ff{__shfl_sync(0xffffffffu, a.hi, src, width), __shfl_sync(0xffffffffu, a.lo, src, width)};
 }
-__device__ __forceinline__ cff cff_shfl(cff a, int src, int width)
+__device__ __forceinline__ cpx_ff cpx_ff_shfl(cpx_ff a, int src, int width)
 {
-    return cff{ff_shfl(a.r, src, width), ff_shfl(a.i, src, width)};
+    return cpx_ff{ff_shfl(a.r, src, width), ff_shfl(a.i, src, width)};
 }
 
 // a x - b y with one renormalisation (19 FP32 operations)
@@ -233,9 +233,9 @@ __device__ __forceinline__ ff ff_fms2(ff a, ff x, ff b, ff y)
     return ff_norm(s, __fadd_rn(t, __fsub_rn(e, f)));
 }
 
-__device__ __forceinline__ cff cff_mul(cff a, cff b)
+__device__ __forceinline__ cpx_ff cpx_ff_mul(cpx_ff a, cpx_ff b)
 {
-    return cff{ff_fms2(a.r, b.r, a.i, b.i), ff_fms2(a.r, b.i, ff{-a.i.hi, -a.i.lo}, b.r)};
+    return cpx_ff{ff_fms2(a.r, b.r, a.i, b.i), ff_fms2(a.r, b.i, ff{-a.i.hi, -a.i.lo}, b.r)};
 }
 
 // acc += x, the rounding error of the high words kept in the low word
@@ -272,10 +272,10 @@ __device__ __forceinline__ ff ff_from_d_scaled(double x, int sh)
 // diagonal (dg1, dg2) and follows the recurrence, each value added to acc[t].
 // ab: this block's coefficient table.
 template <int NT>
-__device__ __forceinline__ void p2x_columns_ff(const float4 *ab, int m1, int len1, int m2, int tot, cff dg1,
-                                               cff dg2, ff zeta, ff eta, ffacc (&ar)[NT], ffacc (&ai)[NT])
+__device__ __forceinline__ void p2x_columns_ff(const float4 *ab, int m1, int len1, int m2, int tot, cpx_ff dg1,
+                                               cpx_ff dg2, ff zeta, ff eta, ffacc (&ar)[NT], ffacc (&ai)[NT])
 {
-    cff x1 = dg1, x2 = cff{ff{0.f, 0.f}, ff{0.f, 0.f}};
+    cpx_ff x1 = dg1, x2 = cpx_ff{ff{0.f, 0.f}, ff{0.f, 0.f}};
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
         if (t >= tot) break;
@@ -284,10 +284,10 @@ __device__ __forceinline__ void p2x_columns_ff(const float4 *ab, int m1, int len
             const int m = second ? m2 : m1, s = second ? t - len1 : t;
             const float4 c = ab[(s > 0 ? s : 1) * kP2xColsMax + m];
             const ff A = ff_mul(ff{c.x, c.y}, zeta), B = ff_mul(ff{c.z, c.w}, eta);
-            cff x = cff{ff_fms2(A, x1.r, B, x2.r), ff_fms2(A, x1.i, B, x2.i)};
+            cpx_ff x = cpx_ff{ff_fms2(A, x1.r, B, x2.r), ff_fms2(A, x1.i, B, x2.i)};
             if (s == 0) {  // the second column's diagonal
                 x = dg2;
-                x1 = cff{ff{0.f, 0.f}, ff{0.f, 0.f}};
+                x1 = cpx_ff{ff{0.f, 0.f}, ff{0.f, 0.f}};
             }
             x2 = x1;
             x1 = x;
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(128) k_p2x_ff(int kind, int P, long long nexp,
     for (unsigned c0 = 0; c0 < cntw; c0 += LP) {
         // this lane's charge of the chunk
         ff zeta{0.f, 0.f}, eta{0.f, 0.f}, w{0.f, 0.f};
-        cff v{ff{0.f, 0.f}, ff{0.f, 0.f}};
+        cpx_ff v{ff{0.f, 0.f}, ff{0.f, 0.f}};
         if (c0 + l < cnt) {
             const long long k = kb + c0 + l;
             const double *pp = pos + 3 * k;
@@ -376,31 +376,31 @@ __global__ void __launch_bounds__(128) k_p2x_ff(int kind, int P, long long nexp,
             if (kind == 0) {
                 zeta = z;
                 eta = r2;
-                v = cff{x, y};
+                v = cpx_ff{x, y};
             } else {
                 const ff ri = ff_rcp(r2);
                 zeta = ff_mul(z, ri);
                 eta = ri;
-                v = cff{ff_mul(x, ri), ff_mul(y, ri)};
+                v = cpx_ff{ff_mul(x, ri), ff_mul(y, ri)};
                 w = ff_mul(w, ff_sqrt(ri));  // U_0^0 = 1/|x'|
             }
         }
         for (int i = 0; i < LP; ++i) {
             const ff zi = ff_shfl(zeta, i, LP), ei = ff_shfl(eta, i, LP), wi = ff_shfl(w, i, LP);
-            const cff vi = cff_shfl(v, i, LP);
+            const cpx_ff vi = cpx_ff_shfl(v, i, LP);
             // v^l by a prefix product over the lanes; v^m2 = v^(P-LP) v^(LP-1-l)
-            cff pw = l == 0 ? cff{ff{1.f, 0.f}, ff{0.f, 0.f}} : vi;
+            cpx_ff pw = l == 0 ? cpx_ff{ff{1.f, 0.f}, ff{0.f, 0.f}} : vi;
 #pragma unroll
             for (int d = 1; d < LP; d <<= 1) {
-                const cff o = cff_shfl(pw, l >= d ? l - d : l, LP);
-                if (l >= d) pw = cff_mul(pw, o);
+                const cpx_ff o = cpx_ff_shfl(pw, l >= d ? l - d : l, LP);
+                if (l >= d) pw = cpx_ff_mul(pw, o);
             }
-            cff ue = cff_shfl(pw, e < LP ? e : LP - 1, LP);
-            if (e == LP) ue = cff_mul(ue, vi);
-            const cff pm2 = cff_mul(ue, cff_shfl(pw, LP - 1 - l, LP));
+            cpx_ff ue = cpx_ff_shfl(pw, e < LP ? e : LP - 1, LP);
+            if (e == LP) ue = cpx_ff_mul(ue, vi);
+            const cpx_ff pm2 = cpx_ff_mul(ue, cpx_ff_shfl(pw, LP - 1 - l, LP));
             const ff k1 = ff_mul(d1, wi), k2 = ff_mul(d2, wi);
-            p2x_columns_ff<NT>(ab, m1, len1, m2, tot, cff{ff_mul(pw.r, k1), ff_mul(pw.i, k1)},
-                               cff{ff_mul(pm2.r, k2), ff_mul(pm2.i, k2)}, zi, ei, ar, ai);
+            p2x_columns_ff<NT>(ab, m1, len1, m2, tot, cpx_ff{ff_mul(pw.r, k1), ff_mul(pw.i, k1)},
+                               cpx_ff{ff_mul(pm2.r, k2), ff_mul(pm2.i, k2)}, zi, ei, ar, ai);
         }
     }
     if (!tot) return;

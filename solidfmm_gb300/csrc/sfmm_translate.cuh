@@ -577,6 +577,14 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
     static_assert(32 % G == 0, "a translation's threads must share a warp");
     static_assert(!FIX || AR::split, "fixed-point swaps are a float-float variant");
 
+    // Loads in flight per lane in the source gather and the target update,
+    // measured on GB300 (M2L P=16, 10^6): 8 and 4 make the split kernel 2.2%
+    // and the FP32 kernel 3.7% faster than 4 and 1, which the FP64 and
+    // float-float kernels keep (1.5% and 0.7% slower with 8 and 4).
+    constexpr bool kDeep = FIX || std::is_same<A, float>::value;
+    constexpr int kGatherUnroll = kDeep ? 8 : 4;
+    constexpr int kAccUnroll = kDeep ? 4 : 1;
+
     extern __shared__ __align__(16) unsigned char smem[];
     const int TS = p.TS;
     const int tid = threadIdx.x;
@@ -687,8 +695,8 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             const Src *sp = p.src_ptr ? reinterpret_cast<const Src *>(p.src_ptr[m_sidx[s]])
                                       : src + (long long)m_sidx[s] * p.sstride;
             S *bp = buf0 + (long long)s * p.spad;
-            if constexpr (HBM) {  // four loads in flight per lane
-#pragma unroll 4
+            if constexpr (HBM) {  // kGatherUnroll loads in flight per lane
+#pragma unroll(kGatherUnroll)
                 for (int c = lane; c < p.spad; c += 32)
                     AR::st(bp + c, c < cnt ? AR::from_src(__ldcs(sp + c)) : AR::zero());
             } else {
@@ -812,9 +820,12 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             const Src *sp = p.src_ptr ? reinterpret_cast<const Src *>(p.src_ptr[m_sidx[s]])
                                       : src + (long long)m_sidx[s] * p.sstride;
             Src *dp = p.dst_ptr ? reinterpret_cast<Src *>(p.dst_ptr[m_tidx[s]]) : dst + (long long)m_tidx[s] * p.dstride;
+#pragma unroll(kAccUnroll)
             for (int c = lane; c < cnt; c += 32) {
                 if constexpr (AR::split) {
                     // hi and lo widen by exponent re-biasing; two FP64 additions
+                    // (one FP64 addition after an integer-only hi + lo measured
+                    // 2% slower: the kernel is issue bound, not FP64 bound)
                     double v = p.atomic ? 0.0 : (double)__ldcs(dp + c);
                     if (c < po * (po + 1)) {
                         const T t = AR::ld(bp + c);
