@@ -409,8 +409,8 @@ def extras(args, local):
     r = run_fmm(sub, nested=True)
     out["c4_fmm"] = {k: r[k] for k in ("value", "unit", "plain_fp64_ms_per_pass", "translations_per_s",
                                        "leaf_local_rel_err_vs_oracle_pass",
-                                       "potential_rel_err_vs_direct_2000_particles", "cpu_baseline",
-                                       "config")} if r else None
+                                       "potential_rel_err_vs_direct_2000_particles", "tensor_core_passes",
+                                       "cpu_baseline", "config")} if r else None
     torch.cuda.empty_cache()
     out["seconds"] = time.perf_counter() - t0
     return out
@@ -679,6 +679,9 @@ def run_fmm(args, nested=False):
     q, pos = fmm.random_particles(depth, per, 900 + rank, dev)
     f = fmm.UniformFMM(ctx, depth, sf.SPLIT, dev)
     fp = fmm.UniformFMM(ctx, depth, sf.PLAIN, dev)
+    # the same pass with every translation on the tensor-core kernel
+    ftc = {name: fmm.UniformFMM(ctx, depth, mode, dev)
+           for name, mode in (("tc_bf16x6", sf.TC_BF16X6), ("tc_tf32x3", sf.TC_TF32), ("tc_bf16x3", sf.TC_BF16))}
     counts = f.translations
     ntr = sum(counts.values())
 
@@ -703,18 +706,16 @@ def run_fmm(args, nested=False):
     ms, launches = timed(f, args.steps, args.warmup)
     clk = clocks.stop()
     ms_plain, _ = timed(fp, max(2, args.steps // 2), 1)
+    ms_tc = {name: timed(obj, max(2, args.steps // 2), 1)[0] for name, obj in ftc.items()}
     if rank != 0:
         return
     # physics: potential at sampled particles, far field (L2P) + near field vs direct sum
-    f.run(q, pos)
     nleaf = 8 ** depth
     g = torch.Generator(device=dev)
     g.manual_seed(5)
     samp = torch.randint(0, nleaf * per, (2000,), device=dev, generator=g)
     pts = pos.reshape(-1, 3)[samp].contiguous()
     box = (samp // per).to(torch.int32)
-    pot = torch.zeros(len(samp), dtype=torch.float64, device=dev)
-    ctx.evaluate(0, len(samp), pts, f.leaf_locals(), f.S, nleaf, f.leaf_centres, pot, box=box)
     allp = pos.reshape(-1, 3)
     allq = q.reshape(-1)
     direct = torch.zeros(len(samp), dtype=torch.float64, device=dev)
@@ -730,7 +731,15 @@ def run_fmm(args, nested=False):
         idx = (srcb[:, None] * per + torch.arange(per, device=dev)[None, :]).reshape(-1)
         r = torch.linalg.norm(allp[idx] - pts[i], dim=1)
         near[i] = torch.where(r > 0, allq[idx] / r.clamp_min(1e-300), torch.zeros_like(r)).sum()
-    phys = float(torch.linalg.norm(pot + near - direct) / torch.linalg.norm(direct))
+    def potential_err(obj):
+        obj.run(q, pos)
+        pot = torch.zeros(len(samp), dtype=torch.float64, device=dev)
+        ctx.evaluate(0, len(samp), pts, obj.leaf_locals(), obj.S, nleaf, obj.leaf_centres, pot, box=box)
+        return float(torch.linalg.norm(pot + near - direct) / torch.linalg.norm(direct))
+
+    phys_tc = {name: potential_err(obj) for name, obj in ftc.items()}
+    phys_plain = potential_err(fp)
+    phys = potential_err(f)
     # leaf locals against the oracle's CPU pass
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import fmm_oracle
@@ -750,6 +759,13 @@ def run_fmm(args, nested=False):
     fp.run(q, pos)
     torch.cuda.synchronize()
     err_plain = rel_err(fp.leaf_locals().cpu().numpy(), ref, w)
+    tc_rows = {}
+    for name, obj in ftc.items():
+        obj.run(q, pos)
+        torch.cuda.synchronize()
+        tc_rows[name] = {"ms_per_pass": ms_tc[name],
+                         "leaf_local_rel_err_vs_oracle_pass": rel_err(obj.leaf_locals().cpu().numpy(), ref, w),
+                         "potential_rel_err_vs_direct_2000_particles": phys_tc[name]}
     line = {"metric": FMM_METRIC, "value": ms, "unit": "ms per pass", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "split (int32 block fixed point rotations, float-float z-translation, "
@@ -762,6 +778,10 @@ def run_fmm(args, nested=False):
             "leaf_local_rel_err_vs_oracle_pass": {"split": err_split, "plain_fp64": err_plain,
                                                    "metric": "max over leaves, relative L2, orthonormal basis"},
             "potential_rel_err_vs_direct_2000_particles": phys,
+            "potential_rel_err_vs_direct_plain_fp64": phys_plain,
+            "tensor_core_passes": tc_rows,
+            "tensor_core_note": "the same pass with every translation (M2M, M2L, L2L) on the tcgen05 kernel; "
+                                "at P=12 the expansion's own truncation error sets the potential error",
             "cpu_baseline": {"value": cpu_s * 1e3, "unit": "ms per pass", "cores": threads, "kind": "port",
                              "sample": "the same pass (P2M + all translations) by the oracle's FP64 rotation-method "
                                        "port, one pthread per core"},
