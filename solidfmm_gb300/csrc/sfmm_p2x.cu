@@ -4,7 +4,7 @@
 // fmadd(q, harmonics::R/S(P, x - c), E) (solid.cpp:70-104) with the R and S
 // recurrences of harmonics.cpp:32-80 and :177-224, evaluated column by column
 // (fixed m, increasing n) so that each coefficient is accumulated as soon as
-// it is produced.  Orders up to 24: float-float arithmetic on the FP32 pipe,
+// it is produced.  Orders up to 32: float-float arithmetic on the FP32 pipe,
 // lanes owning column pairs (k_p2x_ff); above, one FP64 thread per expansion.
 //
 // Bucketing: a counting sort of translation indices by the key
@@ -110,7 +110,7 @@ __global__ void k_p2x(int kind, int P, long long nexp, long long nq, const uint3
     }
 }
 
-// ---- float-float P2M / P2L for order bounds up to 24 ----
+// ---- float-float P2M / P2L for order bounds up to 32 ----
 //
 // The same sums on the FP32 pipe.  Coordinates are scaled by a power of two
 // rho per expansion (x' = (x - c) / rho, |x'| <= 1 for P2M from the farthest
@@ -137,7 +137,7 @@ __global__ void k_p2x(int kind, int P, long long nexp, long long nq, const uint3
 // broadcast by shuffles; the diagonals v^m come from a prefix product across
 // the lanes; the harmonics accumulate in registers and are added to the
 // expansion once.
-constexpr int kP2xColsMax = 24;
+constexpr int kP2xColsMax = 32;
 
 // Tables, evaluated at compile time in FP64: coefficient pairs [s][m] for
 // n = m + s as (a.hi, a.lo, b.hi, b.lo), the diagonal constants
@@ -269,15 +269,16 @@ __device__ __forceinline__ ff ff_from_d_scaled(double x, int sh)
 
 // A lane's two columns as one run of P + 1 harmonics: column m1 at t < len1
 // (t = n - m1), then column m2 at t = len1 + n - m2.  X starts at each
-// diagonal (dg1, dg2) and follows the recurrence, each value added to acc[t].
-// ab: this block's coefficient table.
-template <int NT>
+// diagonal (dg1, dg2) and follows the recurrence; the values of the window
+// T0 <= t < T0 + NT are added to acc[t - T0].  ab: this block's coefficient
+// table.
+template <int T0, int NT>
 __device__ __forceinline__ void p2x_columns_ff(const float4 *ab, int m1, int len1, int m2, int tot, cpx_ff dg1,
                                                cpx_ff dg2, ff zeta, ff eta, ffacc (&ar)[NT], ffacc (&ai)[NT])
 {
     cpx_ff x1 = dg1, x2 = cpx_ff{ff{0.f, 0.f}, ff{0.f, 0.f}};
 #pragma unroll
-    for (int t = 0; t < NT; ++t) {
+    for (int t = 0; t < T0 + NT; ++t) {
         if (t >= tot) break;
         if (t > 0) {
             const bool second = t >= len1;
@@ -292,8 +293,10 @@ __device__ __forceinline__ void p2x_columns_ff(const float4 *ab, int m1, int len
             x2 = x1;
             x1 = x;
         }
-        ffacc_add(ar[t], x1.r);
-        ffacc_add(ai[t], x1.i);
+        if (t >= T0) {
+            ffacc_add(ar[t - T0], x1.r);
+            ffacc_add(ai[t - T0], x1.i);
+        }
     }
 }
 
@@ -306,14 +309,15 @@ __device__ __forceinline__ void p2x_put(Out *o, int kind, int sh, int n, int m, 
     o[(n + 1) * (n + 1) + m] += (Out)(((double)im.hi + (double)im.lo) * f);
 }
 
-template <class Out, int LP>
+// Harmonics T0 .. T0 + NT - 1 of every lane's run (NT = 2 LP + 1 covers all
+// of them; orders above 24 take two windows, two launches, to stay within
+// the registers).
+template <class Out, int LP, int T0, int NT>
 __global__ void __launch_bounds__(128) k_p2x_ff(int kind, int P, long long nexp, long long nq,
                                                 const uint32_t *__restrict__ offset, const double *__restrict__ q,
                                                 const double *__restrict__ pos, const double *__restrict__ centre,
                                                 Out *out, long long stride)
 {
-    // P + 1 <= 2 LP + 1 harmonics per lane
-    constexpr int NT = (2 * LP < kP2xColsMax ? 2 * LP : kP2xColsMax) + 1;
     __shared__ float4 ab[kP2xColsMax * kP2xColsMax];
     for (int i = threadIdx.x; i < P * kP2xColsMax; i += blockDim.x) ab[i] = (&kP2xTab.ab[0][0])[i];
     __syncthreads();
@@ -399,19 +403,21 @@ __global__ void __launch_bounds__(128) k_p2x_ff(int kind, int P, long long nexp,
             if (e == LP) ue = cpx_ff_mul(ue, vi);
             const cpx_ff pm2 = cpx_ff_mul(ue, cpx_ff_shfl(pw, LP - 1 - l, LP));
             const ff k1 = ff_mul(d1, wi), k2 = ff_mul(d2, wi);
-            p2x_columns_ff<NT>(ab, m1, len1, m2, tot, cpx_ff{ff_mul(pw.r, k1), ff_mul(pw.i, k1)},
+            p2x_columns_ff<T0, NT>(ab, m1, len1, m2, tot, cpx_ff{ff_mul(pw.r, k1), ff_mul(pw.i, k1)},
                                cpx_ff{ff_mul(pm2.r, k2), ff_mul(pm2.i, k2)}, zi, ei, ar, ai);
         }
     }
-    if (!tot) return;
+    if (tot <= T0) return;
     // back to R_n^m(x) = rho^n T / sig (P2M) or S_n^m(x) = sig U / rho^(n+1) (P2L)
     Out *o = out + j * stride;
 #pragma unroll
-    for (int t = 0; t < NT; ++t)
+    for (int u = 0; u < NT; ++u) {
+        const int t = T0 + u;
         if (t < tot) {
-            if (t < len1) p2x_put(o, kind, sh, m1 + t, m1, ar[t], ai[t]);
-            else p2x_put(o, kind, sh, m2 + t - len1, m2, ar[t], ai[t]);
+            if (t < len1) p2x_put(o, kind, sh, m1 + t, m1, ar[u], ai[u]);
+            else p2x_put(o, kind, sh, m2 + t - len1, m2, ar[u], ai[u]);
         }
+    }
 }
 
 cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, const uint32_t *offset,
@@ -424,15 +430,22 @@ cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, 
         const int tb = 128;
         const long long grid = (nexp * LP + tb - 1) / tb;
         clear_stale_error();
-#define SFMM_P2X_FF(T, L) k_p2x_ff<T, L><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, offset, q, pos, centre, \
-                                                                      (T *)out, stride)
-#define SFMM_P2X_LP(T)              \
-    switch (LP) {                   \
-    case 1: SFMM_P2X_FF(T, 1); break;  \
-    case 2: SFMM_P2X_FF(T, 2); break;  \
-    case 4: SFMM_P2X_FF(T, 4); break;  \
-    case 8: SFMM_P2X_FF(T, 8); break;  \
-    default: SFMM_P2X_FF(T, 16); break; \
+#define SFMM_P2X_FF(T, L, T0, NT)                                                                        \
+    k_p2x_ff<T, L, T0, NT><<<(unsigned)grid, tb, 0, st>>>(kind, P, nexp, nq, offset, q, pos, centre, (T *)out, \
+                                                          stride)
+#define SFMM_P2X_LP(T)                       \
+    switch (LP) {                            \
+    case 1: SFMM_P2X_FF(T, 1, 0, 3); break;  \
+    case 2: SFMM_P2X_FF(T, 2, 0, 5); break;  \
+    case 4: SFMM_P2X_FF(T, 4, 0, 9); break;  \
+    case 8: SFMM_P2X_FF(T, 8, 0, 17); break; \
+    default:                                 \
+        if (P <= 24) {                       \
+            SFMM_P2X_FF(T, 16, 0, 25);       \
+        } else {                             \
+            SFMM_P2X_FF(T, 16, 0, 17);       \
+            SFMM_P2X_FF(T, 16, 17, 16);      \
+        }                                    \
     }
         if (f64) SFMM_P2X_LP(double) else SFMM_P2X_LP(float)
 #undef SFMM_P2X_LP
