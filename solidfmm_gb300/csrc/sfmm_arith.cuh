@@ -115,27 +115,31 @@ __device__ __forceinline__ float ldexp2(float x, int e)
     return __fmul_rn(__fmul_rn(x, pow2f(e1)), pow2f(e - e1));
 }
 
-// double -> float-float with integer and FP32 operations only (the FP64
+// x 2^sh as float-float with integer and FP32 operations only (the FP64
 // pipe is 1/64 of the FP32 rate).  The 53-bit significand M splits into its
 // top 24 bits A (exact in a float) and the remaining 29 bits B (rounded to 24
-// bits); x = A 2^k + B 2^(k-29), then one Fast2Sum.  The pair represents x to
-// about 2^-48 relative; |x| < 2^-151 becomes 0 and |x| >= 2^128 overflows.
-__device__ __forceinline__ ff ff_from_d_int(double x)
+// bits); x 2^sh = A 2^k + B 2^(k-29), the shift folded into k, then one
+// Fast2Sum.  The pair represents x 2^sh to about 2^-48 relative; results
+// below 2^-151 become 0, from 2^128 they overflow.
+__device__ __forceinline__ ff ff_from_d_scaled(double x, int sh)
 {
     const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
     const int e = (int)((hw >> 20) & 0x7ffu);
     const unsigned A = 0x800000u | ((hw & 0xfffffu) << 3) | (lw >> 29);
     const unsigned B = lw & 0x1fffffffu;
-    const int k = min(e - 1023 - 23, 106);
+    const int k = min(e - 1023 - 23 + sh, 106);
     float h = ldexp2(__uint2float_rn(A), k);
     float l = ldexp2(__uint2float_rn(B), k - 29);
-    if (e < 1023 - 151) h = l = 0.f;
+    if (e - 1023 + sh < -151) h = l = 0.f;  // zero and subnormal x too, for |sh| < 872
     if (hw >> 31) {
         h = -h;
         l = -l;
     }
     return ff_norm(h, l);
 }
+
+// double -> float-float without FP64 instructions
+__device__ __forceinline__ ff ff_from_d_int(double x) { return ff_from_d_scaled(x, 0); }
 
 // float -> double by re-biasing the exponent (exact); zero included, other
 // non-normal values take the conversion instruction.

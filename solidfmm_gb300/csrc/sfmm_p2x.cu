@@ -248,25 +248,6 @@ __device__ __forceinline__ void ffacc_add(ffacc &a, ff x)
     a.lo = __fadd_rn(a.lo, __fadd_rn(e, x.lo));
 }
 
-// x 2^sh as float-float, integer and FP32 operations only (ff_from_d_int with
-// the shift folded into the exponent); |x 2^sh| < 2^-151 becomes 0.
-__device__ __forceinline__ ff ff_from_d_scaled(double x, int sh)
-{
-    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
-    const int e = (int)((hw >> 20) & 0x7ffu);
-    const unsigned A = 0x800000u | ((hw & 0xfffffu) << 3) | (lw >> 29);
-    const unsigned B = lw & 0x1fffffffu;
-    const int k = min(e - 1023 - 23 + sh, 106);
-    float h = ldexp2(__uint2float_rn(A), k);
-    float l = ldexp2(__uint2float_rn(B), k - 29);
-    if (e == 0 || e - 1023 + sh < -151) h = l = 0.f;
-    if (hw >> 31) {
-        h = -h;
-        l = -l;
-    }
-    return ff_norm(h, l);
-}
-
 // A lane's two columns as one run of P + 1 harmonics: column m1 at t < len1
 // (t = n - m1), then column m2 at t = len1 + n - m2.  X starts at each
 // diagonal (dg1, dg2) and follows the recurrence; the values of the window
