@@ -410,6 +410,7 @@ def extras(args, local):
     out["c4_fmm"] = {k: r[k] for k in ("value", "unit", "plain_fp64_ms_per_pass", "translations_per_s",
                                        "leaf_local_rel_err_vs_oracle_pass",
                                        "potential_rel_err_vs_direct_2000_particles", "tensor_core_passes",
+                                       "l2p_gradient_all_particles",
                                        "cpu_baseline", "config")} if r else None
     torch.cuda.empty_cache()
     out["seconds"] = time.perf_counter() - t0
@@ -707,6 +708,21 @@ def run_fmm(args, nested=False):
     clk = clocks.stop()
     ms_plain, _ = timed(fp, max(2, args.steps // 2), 1)
     ms_tc = {name: timed(obj, max(2, args.steps // 2), 1)[0] for name, obj in ftc.items()}
+    # L2P with gradients at every particle from the leaf locals (the step after the pass)
+    nleaf_all = 8 ** depth
+    pts_all = pos.reshape(-1, 3).contiguous()
+    box_all = torch.arange(nleaf_all, device=dev, dtype=torch.int32).repeat_interleave(per)
+    pot_all = torch.zeros(len(pts_all), dtype=torch.float64, device=dev)
+    grad_all = torch.zeros(len(pts_all), 3, dtype=torch.float64, device=dev)
+
+    class _L2P:
+        @staticmethod
+        def run(_q, _pos):
+            ctx.evaluate(0, len(pts_all), pts_all, f.leaf_locals(), f.S, nleaf_all, f.leaf_centres, pot_all,
+                         gradient=grad_all, box=box_all)
+
+    f.run(q, pos)
+    ms_l2p, _ = timed(_L2P, max(2, args.steps), 2)
     if rank != 0:
         return
     # physics: potential at sampled particles, far field (L2P) + near field vs direct sum
@@ -779,6 +795,10 @@ def run_fmm(args, nested=False):
                                                    "metric": "max over leaves, relative L2, orthonormal basis"},
             "potential_rel_err_vs_direct_2000_particles": phys,
             "potential_rel_err_vs_direct_plain_fp64": phys_plain,
+            "l2p_gradient_all_particles": {"ms": ms_l2p, "points": nleaf_all * per,
+                                           "points_per_s": nleaf_all * per / (ms_l2p * 1e-3),
+                                           "what": "sfmm_eval_device: potential and gradient of the leaf "
+                                                   "locals at every particle (float-float, after the pass)"},
             "tensor_core_passes": tc_rows,
             "tensor_core_note": "the same pass with every translation (M2M, M2L, L2L) on the tcgen05 kernel; "
                                 "at P=12 the expansion's own truncation error sets the potential error",

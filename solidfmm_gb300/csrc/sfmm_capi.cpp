@@ -503,6 +503,7 @@ void sfmm_destroy(sfmm_context *c)
         if (c->pipe[k]) cudaStreamDestroy(c->pipe[k]);
     }
     c->d_work.release();
+    c->d_eval.release();
     if (c->d_status) cudaFree(c->d_status);
     free_offsets(c);
     c->h_src.release();
@@ -799,8 +800,23 @@ int sfmm_eval_device(sfmm_context *c, int kind, size_t npts, const double *pos, 
     if (gradient && kind != 0) return fail(c, SFMM_UNSUPPORTED, "gradients are evaluated for local expansions");
     if (!box && nexp < npts) return fail(c, SFMM_INVALID_ARG, "fewer expansions than points without a box index");
     cudaSetDevice(c->device);
+    // float-float needs a scratch copy of the expansions: allocated (or
+    // grown) outside stream capture; a captured call without enough of it
+    // runs the FP64 kernel
+    std::lock_guard<std::mutex> lk(c->eval_mtx);  // calls share the scratch, in stream order
+    void *scratch = nullptr;
+    const size_t need = eval_scratch_bytes(c->P, (long long)nexp);
+    if (need) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(c->stream, &cs);
+        if (cs == cudaStreamCaptureStatusNone && c->d_eval.ensure(need) != cudaSuccess) {
+            clear_stale_error();
+            return fail(c, SFMM_OOM, "L2P/M2P scratch (%zu bytes)", need);
+        }
+        if (c->d_eval.bytes >= need) scratch = c->d_eval.p;
+    }
     cudaError_t e = launch_eval(c->dtype == SFMM_F64, kind, c->P, (long long)npts, pos, box, E, (long long)stride,
-                                centre, potential, gradient, c->stream);
+                                (long long)nexp, centre, potential, gradient, scratch, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "L2P/M2P kernel");
     c->launches++;
     return SFMM_OK;

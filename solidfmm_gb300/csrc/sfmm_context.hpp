@@ -88,9 +88,11 @@ struct sfmm_context {
     std::atomic<uint64_t> launches{0};
     std::mutex mtx;  // serialises host-path calls (one translator object, one stream)
     std::mutex setup_mtx;  // table uploads and the launch-shape cache (device calls may come from several threads)
+    std::mutex eval_mtx;   // the L2P/M2P scratch (d_eval): sized and used by one call at a time
     int *d_status = nullptr;  // device error word of the translation kernels
     // host-path staging (three pipeline slots for the packed host call)
     sfmm::DevBuf d_src[3], d_dst[3], d_meta[3], d_shift[3], d_work;
+    sfmm::DevBuf d_eval;  // normalised expansions of the float-float L2P/M2P
     sfmm::HostBuf h_src, h_dst, h_meta, h_shift;
     cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
     std::map<std::pair<int, int>, sfmm::LaunchShape> shapes;  // (arith, order bound) -> launch shape

@@ -70,10 +70,13 @@ cudaError_t launch_p2x(bool f64, int kind, int P, long long nexp, long long nq, 
                        const double *q, const double *pos, const double *centre, void *out, long long stride,
                        cudaStream_t st);
 
-// L2P / M2P evaluation (sfmm_p2x.cu)
+// L2P / M2P evaluation (sfmm_p2x.cu): float-float over normalised copies of
+// the nexp expansions in `scratch` (eval_scratch_bytes of it) for orders up
+// to 32, else (scratch null or higher orders) one FP64 thread per point.
+size_t eval_scratch_bytes(int P, long long nexp);
 cudaError_t launch_eval(bool f64, int kind, int P, long long npts, const double *pos, const uint32_t *box,
-                        const void *E, long long stride, const double *centre, double *pot, double *grad,
-                        cudaStream_t st);
+                        const void *E, long long stride, long long nexp, const double *centre, double *pot,
+                        double *grad, void *scratch, cudaStream_t st);
 
 // target[j] += slots[j] for unique host targets given by address (sfmm_p2x.cu)
 cudaError_t launch_add_slots(bool f64, long long nt, const unsigned long long *tptr, const uint32_t *cnt,

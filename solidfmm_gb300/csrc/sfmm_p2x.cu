@@ -141,12 +141,18 @@ constexpr int kP2xColsMax = 32;
 
 // Tables, evaluated at compile time in FP64: coefficient pairs [s][m] for
 // n = m + s as (a.hi, a.lo, b.hi, b.lo), the diagonal constants
-// d_1 ... d_m as float-float, sig(n, m) and 1/sig(n, m) at n(n+1)/2 + m.
+// d_1 ... d_m as float-float, and at n(n+1)/2 + m: sig(n, m) and 1/sig(n, m),
+// sig as fs 2^se with fs in [1, 2) and fi = 1/fs (float-float), and the
+// ratios sig(n+1, m')/sig(n, m) for m' = m, m+1, m-1 (float-float).
+constexpr int kP2xNC = kP2xColsMax * (kP2xColsMax + 1) / 2;
 struct P2xTables {
     float4 ab[kP2xColsMax][kP2xColsMax];
     float2 diag[kP2xColsMax];
-    double sig[kP2xColsMax * (kP2xColsMax + 1) / 2];
-    double isig[kP2xColsMax * (kP2xColsMax + 1) / 2];
+    double sig[kP2xNC];
+    double isig[kP2xNC];
+    int se[kP2xNC];
+    float2 fs[kP2xNC], fi[kP2xNC];
+    float2 cz[kP2xNC], cp[kP2xNC], cm[kP2xNC];
 };
 
 namespace p2x_tables {
@@ -192,9 +198,22 @@ constexpr P2xTables make()
                 const float2 b = split(csqrt((double)(n + m - 1) * (double)(n - m - 1) / nm));
                 t.ab[s][m] = float4{a.x, a.y, b.x, b.y};
             }
+            const int ix = n * (n + 1) / 2 + m;
             const double sg = csqrt(fact(n + m) * fact(n - m));
-            t.sig[n * (n + 1) / 2 + m] = sg;
-            t.isig[n * (n + 1) / 2 + m] = 1.0 / sg;
+            t.sig[ix] = sg;
+            t.isig[ix] = 1.0 / sg;
+            double f = sg;  // sig = f 2^e, f in [1, 2) (exact halvings)
+            int e = 0;
+            while (f >= 2.0) {
+                f *= 0.5;
+                ++e;
+            }
+            t.se[ix] = e;
+            t.fs[ix] = split(f);
+            t.fi[ix] = split(1.0 / f);
+            t.cz[ix] = split(csqrt((double)(n + 1 + m) * (double)(n + 1 - m)));
+            t.cp[ix] = split(csqrt((double)(n + m + 1) * (double)(n + m + 2)));
+            t.cm[ix] = split(m > 0 ? csqrt((double)(n - m + 1) * (double)(n - m + 2)) : 0.0);
         }
     }
     return t;
@@ -556,14 +575,211 @@ __global__ void k_eval(int kind, int P, long long npts, const double *__restrict
     }
 }
 
+// ---- float-float L2P / M2P for orders up to 32 ----
+//
+// The same sums as k_eval on the FP32 pipe, on the Schmidt-normalised
+// harmonics of P2M/P2L (k_p2x_ff).  A pre-pass (k_eval_prep, one thread per
+// expansion and degree n) writes each coefficient in the matching normalised
+// form, e(n,m) = E(n,m) / sig(n,m) for a local expansion or E(n,m) sig(n,m)
+// for a multipole, as float-float mantissas at one block exponent per degree
+// (e = M 2^s_n, |M| < 4), so that evaluating a point costs an exponent shift
+// per coefficient instead of a conversion.  Per point (k_eval_ff):
+// x' = (x - c) / rho, rho = 2^sh rounded up from |x - c| for L2P (|x'| <= 1)
+// and down for M2P (|x'| >= 1), then
+//   E . R(x - c) = sum_{n,m} w_m (e 2^(n sh)) . T_n^m(x')           (L2P)
+//   E . S(x - c) = sum_{n,m} w_m (e 2^-((n+1) sh)) . U_n^m(x')      (M2P)
+// with w_0 = 1, w_m = 2 (the solid dot product, solid.cpp:41-66).  The
+// gradient of a local expansion pairs T_k^v with the degree-(k+1)
+// coefficients v, v+1, v-1 as k_eval does with R_k^v, each pairing weighted
+// by sig(k+1, v')/sig(k, v), the sum divided by rho.
+
+// binary exponent of x (x = f 2^e, f in [1, 2)); zero and subnormals give a
+// value below every other
+__device__ __forceinline__ int exp_of(double x)
+{
+    const int e = (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu);
+    return e ? e - 1023 : -(1 << 20);
+}
+__device__ __forceinline__ int exp_of(float x)
+{
+    const int e = (int)((__float_as_uint(x) >> 23) & 0xffu);
+    return e ? e - 127 : -(1 << 20);
+}
+__device__ __forceinline__ ff ff_of_scaled(double x, int sh) { return ff_from_d_scaled(x, sh); }
+__device__ __forceinline__ ff ff_of_scaled(float x, int sh) { return ff{ldexp2(x, max(-252, min(252, sh))), 0.f}; }
+
+template <class In>
+__global__ void k_eval_prep(int kind, int P, long long nexp, const In *__restrict__ E, long long stride,
+                            float4 *__restrict__ Mout, int *__restrict__ sdeg)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nexp * P) return;
+    const long long b = i / P;
+    const int n = (int)(i - b * P);
+    const In *e = E + b * stride;
+    const int t0 = n * (n + 1) / 2;
+    int s = -(1 << 20);
+    for (int m = 0; m <= n; ++m) {
+        const int se = kind ? kP2xTab.se[t0 + m] : -kP2xTab.se[t0 + m];
+        s = max(s, max(exp_of(e[n * (n + 1) + m]), exp_of(e[(n + 1) * (n + 1) + m])) + se);
+    }
+    if (s < -(1 << 19)) s = 0;  // an all-zero degree
+    sdeg[i] = s;
+    float4 *o = Mout + b * (P * (P + 1) / 2) + t0;
+    for (int m = 0; m <= n; ++m) {
+        const int se = kind ? kP2xTab.se[t0 + m] : -kP2xTab.se[t0 + m];
+        const float2 f2 = kind ? kP2xTab.fs[t0 + m] : kP2xTab.fi[t0 + m];
+        const ff f{f2.x, f2.y};
+        const ff re = ff_mul(ff_of_scaled(e[n * (n + 1) + m], se - s), f);
+        const ff im = ff_mul(ff_of_scaled(e[(n + 1) * (n + 1) + m], se - s), f);
+        o[m] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    }
+}
+
+// coefficient (n, m) of expansion row Mb times 2^ex (|M| < 4: beyond +-252
+// the product under- or overflows FP32 in any case)
+__device__ __forceinline__ cpx_ff eval_coef(const float4 *Mb, int n, int m, int ex)
+{
+    ex = max(-252, min(252, ex));
+    const float4 v = __ldg(Mb + n * (n + 1) / 2 + m);
+    return cpx_ff{ff{ldexp2(v.x, ex), ldexp2(v.y, ex)}, ff{ldexp2(v.z, ex), ldexp2(v.w, ex)}};
+}
+__device__ __forceinline__ ff ff_tab(const float2 *t, int i)
+{
+    const float2 v = t[i];
+    return ff{v.x, v.y};
+}
+__device__ __forceinline__ void ffacc_madd(ffacc &a, ff w, ff x) { ffacc_add(a, ff_mul(w, x)); }
+
+__global__ void __launch_bounds__(128) k_eval_ff(int kind, int P, long long npts, const double *__restrict__ pos,
+                                                 const uint32_t *__restrict__ box, const float4 *__restrict__ M,
+                                                 const int *__restrict__ sdeg, const double *__restrict__ centre,
+                                                 double *pot, double *grad)
+{
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= npts) return;
+    const long long b = box ? (long long)box[j] : j;
+    const double dx = pos[3 * j] - centre[3 * b], dy = pos[3 * j + 1] - centre[3 * b + 1],
+                 dz = pos[3 * j + 2] - centre[3 * b + 2];
+    // rho = 2^sh: rho^2 >= |x - c|^2 (L2P) or rho^2 <= |x - c|^2 / 2 (M2P)
+    const float r2f = (float)(dx * dx + dy * dy + dz * dz);
+    int sh = 0;
+    if (r2f > 0.f && r2f < __int_as_float(0x7f800000)) {
+        int Ex;
+        frexpf(r2f, &Ex);
+        sh = max(-100, min(100, kind == 0 ? (Ex + 1) >> 1 : (Ex - 1) >> 1));
+    }
+    const ff x = ff_from_d_scaled(dx, -sh), y = ff_from_d_scaled(dy, -sh), z = ff_from_d_scaled(dz, -sh);
+    const ff r2 = ff_add(ff_add(ff_mul(x, x), ff_mul(y, y)), ff_mul(z, z));
+    ff zeta, eta, w0{1.f, 0.f};
+    cpx_ff v;
+    if (kind == 0) {
+        zeta = z;
+        eta = r2;
+        v = cpx_ff{x, y};
+    } else {
+        const ff ri = ff_rcp(r2);
+        zeta = ff_mul(z, ri);
+        eta = ri;
+        v = cpx_ff{ff_mul(x, ri), ff_mul(y, ri)};
+        w0 = ff_sqrt(ri);  // U_0^0 = 1/|x'|
+    }
+    const float4 *Mb = M + b * (P * (P + 1) / 2);
+    const int *sb = sdeg + b * P;
+    const bool want_grad = grad != nullptr && kind == 0;
+    // v^(2^i), i < 5: every v^m (m < 32) is a product of at most five of
+    // them, so its rounding error grows with log m rather than with m
+    cpx_ff v2i[5];
+    v2i[0] = v;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) v2i[i] = cpx_ff_mul(v2i[i - 1], v2i[i - 1]);
+    // each column sums into fresh accumulators (at most P terms), added to
+    // the totals with a renormalising float-float addition
+    ff phi{0.f, 0.f}, gx{0.f, 0.f}, gy{0.f, 0.f}, gz{0.f, 0.f};
+    for (int m = 0; m < P; ++m) {
+        cpx_ff vm{w0, ff{0.f, 0.f}};  // v^m / |x'| (M2P) or v^m (L2P)
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+            if (m >> i & 1) vm = cpx_ff_mul(vm, v2i[i]);
+        const ff dm = ff_tab(kP2xTab.diag, m);
+        cpx_ff x1{ff_mul(dm, vm.r), ff_mul(dm, vm.i)}, x2{ff{0.f, 0.f}, ff{0.f, 0.f}};
+        ffacc cphi{0.f, 0.f}, cgx{0.f, 0.f}, cgy{0.f, 0.f}, cgz{0.f, 0.f};
+        const float wm = m ? 2.f : 1.f;
+        for (int n = m; n < P; ++n) {
+            if (n > m) {
+                const float4 c = kP2xTab.ab[n - m][m];
+                const ff A = ff_mul(ff{c.x, c.y}, zeta), B = ff_mul(ff{c.z, c.w}, eta);
+                const cpx_ff xn{ff_fms2(A, x1.r, B, x2.r), ff_fms2(A, x1.i, B, x2.i)};
+                x2 = x1;
+                x1 = xn;
+            }
+            const int ex = kind == 0 ? sb[n] + n * sh : sb[n] - (n + 1) * sh;
+            const cpx_ff e = eval_coef(Mb, n, m, ex);
+            const ff t = ff_fms2(e.r, x1.r, ff{-e.i.hi, -e.i.lo}, x1.i);  // e_re X_re + e_im X_im
+            ffacc_add(cphi, ff{t.hi * wm, t.lo * wm});
+            if (want_grad && n + 1 < P) {
+                const int k1 = n + 1, ix = n * (n + 1) / 2 + m, ex1 = sb[k1] + k1 * sh;
+                const cpx_ff ez = eval_coef(Mb, k1, m, ex1);
+                const ff tz = ff_fms2(ez.r, x1.r, ff{-ez.i.hi, -ez.i.lo}, x1.i);
+                ffacc_madd(cgz, ff_tab(kP2xTab.cz, ix), ff{tz.hi * wm, tz.lo * wm});
+                const cpx_ff ep = eval_coef(Mb, k1, m + 1, ex1);
+                const ff cp = ff_tab(kP2xTab.cp, ix);
+                if (m == 0) {  // R_k^0 is real
+                    ffacc_madd(cgx, cp, ff_mul(x1.r, ep.r));
+                    ffacc_madd(cgy, cp, ff_mul(x1.r, ep.i));
+                } else {
+                    const cpx_ff em = eval_coef(Mb, k1, m - 1, ex1);
+                    const ff cm = ff_tab(kP2xTab.cm, ix);
+                    // conj(R) (L^{m+1} - L^{m-1}) and conj(R) (L^{m-1} + L^{m+1}), each L weighted
+                    const ff xr = ff_fms2(cp, ep.r, cm, em.r), xi = ff_fms2(cp, ep.i, cm, em.i);
+                    const ff yr = ff_fms2(cm, em.r, ff{-cp.hi, -cp.lo}, ep.r);
+                    const ff yi = ff_fms2(cm, em.i, ff{-cp.hi, -cp.lo}, ep.i);
+                    ffacc_add(cgx, ff_fms2(x1.r, xr, ff{-x1.i.hi, -x1.i.lo}, xi));
+                    ffacc_add(cgy, ff_fms2(x1.r, yi, x1.i, yr));
+                }
+            }
+        }
+        phi = ff_add(phi, ff{cphi.hi, cphi.lo});
+        if (want_grad) {
+            gx = ff_add(gx, ff{cgx.hi, cgx.lo});
+            gy = ff_add(gy, ff{cgy.hi, cgy.lo});
+            gz = ff_add(gz, ff{cgz.hi, cgz.lo});
+        }
+    }
+    pot[j] += (double)phi.hi + (double)phi.lo;
+    if (want_grad) {
+        const double ir = ldexp(1.0, -sh);
+        grad[3 * j] += ((double)gx.hi + (double)gx.lo) * ir;
+        grad[3 * j + 1] += ((double)gy.hi + (double)gy.lo) * ir;
+        grad[3 * j + 2] += ((double)gz.hi + (double)gz.lo) * ir;
+    }
+}
+
+size_t eval_scratch_bytes(int P, long long nexp)
+{
+    if (P > kP2xColsMax) return 0;
+    return (size_t)nexp * ((size_t)P * (P + 1) / 2 * sizeof(float4) + (size_t)P * sizeof(int));
+}
+
 cudaError_t launch_eval(bool f64, int kind, int P, long long npts, const double *pos, const uint32_t *box,
-                        const void *E, long long stride, const double *centre, double *pot, double *grad,
-                        cudaStream_t st)
+                        const void *E, long long stride, long long nexp, const double *centre, double *pot,
+                        double *grad, void *scratch, cudaStream_t st)
 {
     if (npts == 0) return cudaSuccess;
     const int tb = 128;
     const long long grid = (npts + tb - 1) / tb;
     clear_stale_error();
+    if (scratch && P <= kP2xColsMax) {  // float-float: normalise every expansion once, then the points
+        float4 *Mn = static_cast<float4 *>(scratch);
+        int *sdeg = reinterpret_cast<int *>(Mn + (size_t)nexp * (P * (P + 1) / 2));
+        const long long gp = (nexp * P + tb - 1) / tb;
+        if (f64)
+            k_eval_prep<double><<<(unsigned)gp, tb, 0, st>>>(kind, P, nexp, (const double *)E, stride, Mn, sdeg);
+        else
+            k_eval_prep<float><<<(unsigned)gp, tb, 0, st>>>(kind, P, nexp, (const float *)E, stride, Mn, sdeg);
+        k_eval_ff<<<(unsigned)grid, tb, 0, st>>>(kind, P, npts, pos, box, Mn, sdeg, centre, pot, grad);
+        return cudaGetLastError();
+    }
     if (f64)
         k_eval<double><<<(unsigned)grid, tb, 0, st>>>(kind, P, npts, pos, box, (const double *)E, stride, centre,
                                                        pot, grad);

@@ -7,13 +7,30 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
+# float-float evaluation: error per point over the sum of its terms' magnitudes
+# (measured <= 2.9e-14 at orders 1..32, both kinds)
+TOL_EVAL = 1e-13
+
 
 def _pot(oracle, kind, E, P, pts, centre):
     h = "R" if kind == 0 else "S"
     return np.array([oracle.dot(E, P, oracle.harmonic(h, P, *(p - centre)), P) for p in pts])
 
 
-@pytest.mark.parametrize("P", [1, 6, 12, 20])
+def _pot_abs(oracle, kind, E, P, pts, centre):
+    """Per point, the sum of the absolute values of the dot product's terms,
+    sum w_m (|E_re H_re| + |E_im H_im|): the scale of the rounding errors of a
+    sum whose terms may cancel."""
+    h = "R" if kind == 0 else "S"
+    w = np.ones(P * (P + 1))
+    for n in range(P):
+        w[n * (n + 1) + 1:n * (n + 1) + n + 1] = 2.0
+        w[(n + 1) * (n + 1) + 1:(n + 1) * (n + 1) + n + 1] = 2.0
+    return np.array([np.sum(w * np.abs(E * oracle.harmonic(h, P, *(p - centre)))) for p in pts])
+
+
+# orders up to 32 in float-float over normalised expansions, 33 in FP64
+@pytest.mark.parametrize("P", [1, 2, 6, 12, 20, 24, 32, 33])
 @pytest.mark.parametrize("kind", [0, 1], ids=["l2p", "m2p"])
 def test_eval_matches_oracle(native, oracle, kind, P):
     import torch
@@ -42,13 +59,15 @@ def test_eval_matches_oracle(native, oracle, kind, P):
                  torch.as_tensor(centres, device=dev), pot, box=torch.as_tensor(box.astype(np.int32), device=dev))
     torch.cuda.synchronize()
     got = pot.cpu().numpy()
-    assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref)) + 1e-300
+    # float-float (orders up to 32): error against the terms' magnitudes
+    scale = np.concatenate([_pot_abs(oracle, kind, E[b], P, pts[box == b], centres[b]) for b in range(nexp)])
+    assert np.max(np.abs(got - ref) / scale) <= TOL_EVAL
 
 
-def test_l2p_gradient_is_derivative(native, oracle):
+@pytest.mark.parametrize("P", [12, 25])
+def test_l2p_gradient_is_derivative(native, oracle, P):
     import torch
 
-    P = 12
     rng = np.random.default_rng(3)
     q = rng.choice([-1.0, 1.0], size=(1, 24))
     d = rng.normal(size=(1, 24, 3))
@@ -106,3 +125,81 @@ def test_p2m_m2l_l2p_physics(native):
     field = -(qs[None, :, None] * diff / r[..., None] ** 3).sum(1)  # grad of sum q/r
     assert np.max(np.abs(pot.cpu().numpy() - phi)) < 1e-7 * np.max(np.abs(phi))
     assert np.max(np.abs(grad.cpu().numpy() - field)) < 1e-6 * np.max(np.abs(field))
+
+
+@pytest.mark.parametrize("kind", [0, 1], ids=["l2p", "m2p"])
+def test_eval_fp32_context(native, oracle, kind):
+    """FP32 expansions (an FP32 context) evaluated in float-float."""
+    import torch
+
+    P = 14
+    rng = np.random.default_rng(40 + kind)
+    q = rng.choice([-1.0, 1.0], size=(3, 16))
+    d = rng.normal(size=(3, 16, 3))
+    src = d / np.linalg.norm(d, axis=2, keepdims=True) * 0.4
+    if kind == 0:
+        src = src + np.array([3.0, -1.0, 2.0])
+    centres = np.zeros((3, 3))
+    E = oracle.p2m(P, q, src, centres, singular=(kind == 0)).astype(np.float32)
+    u = rng.normal(size=(90, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    pts = u * (0.4 if kind == 0 else 3.0)
+    box = np.repeat(np.arange(3), 30).astype(np.uint32)
+    ref = np.concatenate([_pot(oracle, kind, E[b].astype(np.float64), P, pts[box == b], centres[b])
+                          for b in range(3)])
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f32")
+    pot = torch.zeros(len(pts), dtype=torch.float64, device=dev)
+    S = P * (P + 1)
+    ctx.evaluate(kind, len(pts), torch.as_tensor(pts, device=dev), torch.as_tensor(E, device=dev), S, 3,
+                 torch.as_tensor(centres, device=dev), pot, box=torch.as_tensor(box.astype(np.int32), device=dev))
+    torch.cuda.synchronize()
+    assert np.max(np.abs(pot.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def _grad_ref(oracle, L, P, pt):
+    """grad of dot(L, R(x)) at x = pt: (d/dx - i d/dy) R_n^m = R_{n-1}^{m-1},
+    (d/dx + i d/dy) R_n^m = -R_{n-1}^{m+1}, d/dz R_n^m = R_{n-1}^m, in FP64
+    over the oracle's R."""
+    R = oracle.harmonic("R", P, *pt)
+    re = lambda n, m: L[n * (n + 1) + m]  # noqa: E731
+    im = lambda n, m: L[(n + 1) * (n + 1) + m]  # noqa: E731
+    g = np.zeros(3)
+    for m in range(P):
+        for n in range(m, P - 1):
+            cr, ci = R[n * (n + 1) + m], R[(n + 1) * (n + 1) + m]
+            k1, w = n + 1, (2.0 if m else 1.0)
+            g[2] += w * (re(k1, m) * cr + im(k1, m) * ci)
+            if m == 0:
+                g[0] += cr * re(k1, 1)
+                g[1] += cr * im(k1, 1)
+            else:
+                xr, xi = re(k1, m + 1) - re(k1, m - 1), im(k1, m + 1) - im(k1, m - 1)
+                yr, yi = re(k1, m - 1) + re(k1, m + 1), im(k1, m - 1) + im(k1, m + 1)
+                g[0] += cr * xr + ci * xi
+                g[1] += cr * yi - ci * yr
+    return g
+
+
+@pytest.mark.parametrize("P", [3, 16, 32])
+def test_l2p_gradient_matches_fp64_formula(native, oracle, P):
+    import torch
+
+    rng = np.random.default_rng(70 + P)
+    q = rng.choice([-1.0, 1.0], size=(2, 20))
+    d = rng.normal(size=(2, 20, 3))
+    src = d / np.linalg.norm(d, axis=2, keepdims=True) * 0.4 + np.array([2.5, 1.0, -1.5])
+    centres = np.array([[0.0, 0.0, 0.0], [0.1, -0.2, 0.05]])
+    L = oracle.p2m(P, q, src + centres[:, None, :], centres, singular=True)
+    box = np.repeat(np.arange(2), 40).astype(np.uint32)
+    pts = rng.normal(size=(80, 3)) * 0.25 + centres[box]
+    ref = np.array([_grad_ref(oracle, L[b], P, p - centres[b]) for p, b in zip(pts, box)])
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    pot = torch.zeros(80, dtype=torch.float64, device=dev)
+    grad = torch.zeros(80, 3, dtype=torch.float64, device=dev)
+    ctx.evaluate(0, 80, torch.as_tensor(pts, device=dev), torch.as_tensor(L, device=dev), P * (P + 1), 2,
+                 torch.as_tensor(centres, device=dev), pot, gradient=grad,
+                 box=torch.as_tensor(box.astype(np.int32), device=dev))
+    torch.cuda.synchronize()
+    assert np.max(np.abs(grad.cpu().numpy() - ref)) <= 1e-12 * np.max(np.abs(ref))
