@@ -203,3 +203,40 @@ def test_l2p_gradient_matches_fp64_formula(native, oracle, P):
                  box=torch.as_tensor(box.astype(np.int32), device=dev))
     torch.cuda.synchronize()
     assert np.max(np.abs(grad.cpu().numpy() - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("warm", [False, True], ids=["fresh-fp64", "scratch-float-float"])
+def test_eval_inside_graph_capture(native, oracle, warm):
+    """A captured evaluation allocates nothing: a fresh context runs the FP64
+    kernel in the graph, one whose scratch exists runs the float-float path;
+    either replay matches the oracle."""
+    import torch
+
+    P, n = 10, 64
+    rng = np.random.default_rng(5)
+    q = rng.choice([-1.0, 1.0], size=(1, 12))
+    d = rng.normal(size=(1, 12, 3))
+    src = d / np.linalg.norm(d, axis=2, keepdims=True) * 0.4 + np.array([2.5, 1.0, -1.5])
+    L = oracle.p2m(P, q, src, np.zeros((1, 3)), singular=True)
+    pts = rng.normal(size=(n, 3)) * 0.2
+    ref = _pot(oracle, 0, L[0], P, pts, np.zeros(3))
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    tp, tL = torch.as_tensor(pts, device=dev), torch.as_tensor(L, device=dev)
+    cen = torch.zeros(1, 3, dtype=torch.float64, device=dev)
+    box = torch.zeros(n, dtype=torch.int32, device=dev)
+    pot = torch.zeros(n, dtype=torch.float64, device=dev)
+    if warm:  # sizes the scratch outside capture
+        ctx.evaluate(0, n, tp, tL, P * (P + 1), 1, cen, pot, box=box)
+        torch.cuda.synchronize()
+    pot.zero_()
+    s = torch.cuda.Stream(device=dev)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ctx.set_stream(s.cuda_stream)
+        ctx.evaluate(0, n, tp, tL, P * (P + 1), 1, cen, pot, box=box)
+    ctx.set_stream(torch.cuda.current_stream(dev).cuda_stream)
+    pot.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert np.max(np.abs(pot.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
