@@ -262,12 +262,13 @@ int sfmm_bucket_by_order_noalloc(size_t n, const uint32_t *p_in, const uint32_t 
  *   potential[j] += dot(E[b], S(pos[j] - centre[b]))    (kind 1, multipole)
  * with dot the reference's solid dot product (solid.cpp:41-66).  For kind 0
  * a non-NULL gradient (3 per point) receives += grad phi(pos[j]) as well.
- * Orders up to 32 run in float-float on the FP32 pipe over a normalised copy
- * of all nexp expansions, made once per call in context scratch of about
+ * Orders up to 32 with at least one point per four expansions run in
+ * float-float on the FP32 pipe over a normalised copy of all nexp
+ * expansions, made once per call in context scratch of about
  * nexp * P(P+1) * 8 bytes (allocated or grown on first need; a call inside a
- * stream capture never allocates and, without enough scratch, runs FP64);
- * error about 1e-14 of the sum of the terms' magnitudes.  Higher orders run
- * in FP64.  Calls on one context share the scratch (serialised by a lock,
+ * stream capture never allocates, and a call without enough scratch runs
+ * FP64); error about 1e-14 of the sum of the terms' magnitudes.  Other calls
+ * run in FP64.  Calls on one context share the scratch (serialised by a lock,
  * ordered on the context's stream).  Box indices are not range-checked
  * (device data). */
 int sfmm_eval_device(sfmm_context *ctx, int kind, size_t npts, const double *pos, const uint32_t *box,

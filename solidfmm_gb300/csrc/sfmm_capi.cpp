@@ -800,19 +800,17 @@ int sfmm_eval_device(sfmm_context *c, int kind, size_t npts, const double *pos, 
     if (gradient && kind != 0) return fail(c, SFMM_UNSUPPORTED, "gradients are evaluated for local expansions");
     if (!box && nexp < npts) return fail(c, SFMM_INVALID_ARG, "fewer expansions than points without a box index");
     cudaSetDevice(c->device);
-    // float-float needs a scratch copy of the expansions: allocated (or
-    // grown) outside stream capture; a captured call without enough of it
-    // runs the FP64 kernel
+    // float-float normalises all nexp expansions into scratch first: worth it
+    // from one point per four expansions on.  The scratch is allocated (or
+    // grown) outside stream capture only; a call without enough of it (in a
+    // capture, or when the allocation fails) runs the FP64 kernel.
     std::lock_guard<std::mutex> lk(c->eval_mtx);  // calls share the scratch, in stream order
     void *scratch = nullptr;
-    const size_t need = eval_scratch_bytes(c->P, (long long)nexp);
+    const size_t need = 4 * npts >= nexp ? eval_scratch_bytes(c->P, (long long)nexp) : 0;
     if (need) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(c->stream, &cs);
-        if (cs == cudaStreamCaptureStatusNone && c->d_eval.ensure(need) != cudaSuccess) {
-            clear_stale_error();
-            return fail(c, SFMM_OOM, "L2P/M2P scratch (%zu bytes)", need);
-        }
+        if (cs == cudaStreamCaptureStatusNone && c->d_eval.ensure(need) != cudaSuccess) clear_stale_error();
         if (c->d_eval.bytes >= need) scratch = c->d_eval.p;
     }
     cudaError_t e = launch_eval(c->dtype == SFMM_F64, kind, c->P, (long long)npts, pos, box, E, (long long)stride,

@@ -240,3 +240,27 @@ def test_eval_inside_graph_capture(native, oracle, warm):
     g.replay()
     torch.cuda.synchronize()
     assert np.max(np.abs(pot.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_eval_few_points_many_expansions(native, oracle):
+    """Fewer than one point per four expansions: no normalised copy of the
+    whole array (the FP64 kernel), same results."""
+    import torch
+
+    P, nexp = 9, 400
+    rng = np.random.default_rng(8)
+    q = rng.choice([-1.0, 1.0], size=(nexp, 6))
+    d = rng.normal(size=(nexp, 6, 3))
+    src = d / np.linalg.norm(d, axis=2, keepdims=True) * 0.4 + np.array([2.5, 1.0, -1.5])
+    L = oracle.p2m(P, q, src, np.zeros((nexp, 3)), singular=True)
+    box = np.array([3, 77, 150, 399, 0, 201], dtype=np.uint32)
+    pts = rng.normal(size=(len(box), 3)) * 0.2
+    ref = np.array([_pot(oracle, 0, L[b], P, pts[i:i + 1], np.zeros(3))[0] for i, b in enumerate(box)])
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    pot = torch.zeros(len(box), dtype=torch.float64, device=dev)
+    ctx.evaluate(0, len(box), torch.as_tensor(pts, device=dev), torch.as_tensor(L, device=dev), P * (P + 1), nexp,
+                 torch.zeros(nexp, 3, dtype=torch.float64, device=dev), pot,
+                 box=torch.as_tensor(box.astype(np.int32), device=dev))
+    torch.cuda.synchronize()
+    assert np.max(np.abs(pot.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
