@@ -264,3 +264,26 @@ def test_eval_few_points_many_expansions(native, oracle):
                  box=torch.as_tensor(box.astype(np.int32), device=dev))
     torch.cuda.synchronize()
     assert np.max(np.abs(pot.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("P", [1, 2, 12])
+def test_l2p_at_the_centre(native, oracle, P):
+    """At the centre only R_0^0 = 1 is nonzero: the potential is L_0^0 and the
+    gradient comes from the degree-1 coefficients alone."""
+    import torch
+
+    rng = np.random.default_rng(P)
+    L = rng.normal(size=(1, P * (P + 1)))
+    for n in range(P):
+        L[0, (n + 1) * (n + 1)] = 0.0  # imaginary part of m = 0
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    pot = torch.zeros(1, dtype=torch.float64, device=dev)
+    grad = torch.zeros(1, 3, dtype=torch.float64, device=dev)
+    c = np.array([[0.25, -0.5, 1.0]])
+    ctx.evaluate(0, 1, torch.as_tensor(c, device=dev), torch.as_tensor(L, device=dev), P * (P + 1), 1,
+                 torch.as_tensor(c, device=dev), pot, gradient=grad)
+    torch.cuda.synchronize()
+    assert pot.item() == pytest.approx(L[0, 0], rel=1e-14, abs=0)
+    ref = _grad_ref(oracle, L[0], P, np.zeros(3))
+    assert np.max(np.abs(grad.cpu().numpy()[0] - ref)) <= 1e-14 * max(np.max(np.abs(ref)), 1e-300)

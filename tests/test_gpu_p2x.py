@@ -160,3 +160,18 @@ def test_many_expansions(native, oracle):
     assert p2x_err(got[pick], ref, P, 0, q[pick], pos[pick], cen[pick]) < TOL_ABS
     assert rel_err(got[pick], ref) < TOL_ABS
     assert schmidt_degree_err(got[pick], ref, P, 0) < TOL_DEG
+
+
+@pytest.mark.parametrize("P", [1, 5, 16, 30])
+def test_p2m_charge_at_the_centre(native, oracle, P):
+    """A charge exactly at the centre adds q to R_0^0 only; the expansion's
+    scale then comes from the other charges (none in the first expansion)."""
+    rng = np.random.default_rng(P)
+    q = np.array([[2.5, 0.0, 0.0], [1.0, -1.0, 0.5]])
+    cen = np.array([[0.3, -0.2, 0.1], [0.0, 0.0, 0.0]])
+    pos = np.repeat(cen[:, None, :], 3, axis=1).copy()
+    pos[1, 1:] += rng.normal(size=(2, 3)) * 0.3
+    ref = oracle.p2m(P, q, pos, cen)
+    got = run_p2x(native, P, 0, q, pos, cen)
+    assert got[0, 0] == 2.5 and np.all(got[0, 1:] == 0)
+    assert p2x_err(got, ref, P, 0, q, pos, cen) < TOL_ABS
