@@ -174,7 +174,7 @@ int sfmm_bounding_sphere(size_t n, const double *x, const double *y, const doubl
  * sfmm_tune times every supported G, each with the largest and the smallest
  * tile (translations per CTA) that keep the SM fully occupied, on n synthetic
  * translations of `op` on the context's stream (synchronising it) and keeps
- * the fastest.  `group`
+ * the fastest for that (op, precision, order bound).  `group`
  * (may be NULL) receives the kept G, `rate` (may be NULL) its measured
  * translations per second.  order_bound 0 = the context order. */
 int sfmm_set_group(sfmm_context *ctx, int precision, size_t order_bound, int group);
@@ -207,11 +207,14 @@ int sfmm_plan_create(sfmm_context *ctx, sfmm_plan **plan);
  * SFMM_PLAN_TUNE   finalize measures launch shapes and launches with the
  *                  fastest: a fused stage's on a synthetic batch with the
  *                  stage's own order distribution (a sample of up to 65 536
- *                  of its translations; the shape stays with the plan), the
- *                  segments' with sfmm_tune (uniform orders, min(max(count,
- *                  4096), 65536) translations) for every (operator,
- *                  precision, order bound) the context has not measured yet
- *                  (the shape stays with the context).
+ *                  of its translations; the shape stays with the plan), each
+ *                  segment's on the segment itself (its sources, indices,
+ *                  orders and shifts, writing into a scratch copy of its
+ *                  target array, so the plan's targets stay untouched; with
+ *                  sfmm_tune's synthetic batch instead when that copy would
+ *                  take more than a quarter of the free device memory), for
+ *                  every (operator, precision, order bound) the context has
+ *                  not measured yet (the shape stays with the context).
  * Default 0: one launch per segment, built-in shapes. */
 enum { SFMM_PLAN_FUSED = 1, SFMM_PLAN_TUNE = 2 };
 int sfmm_plan_set_options(sfmm_plan *plan, int options);

@@ -211,7 +211,7 @@ int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound, LaunchShape *sh
         }
         return SFMM_OK;
     }
-    const auto key = std::make_pair((int)a, Pbound);
+    const auto key = std::make_tuple(op, (int)a, Pbound);
     auto it = c->shapes.find(key);
     if (it == c->shapes.end()) it = c->shapes.emplace(key, best_shape(a, Pbound, default_group(a, Pbound))).first;
     if (shape) *shape = it->second;
@@ -222,8 +222,7 @@ int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound, LaunchShape *sh
     return SFMM_OK;
 }
 
-// replace (or, with nullptr, drop) a cached launch shape
-void set_shape(sfmm_context *c, std::pair<int, int> key, const LaunchShape *s)
+void set_shape(sfmm_context *c, std::tuple<int, int, int> key, const LaunchShape *s)
 {
     std::lock_guard<std::mutex> lk(c->setup_mtx);
     if (s) c->shapes[key] = *s;
@@ -569,10 +568,15 @@ int sfmm_set_group(sfmm_context *c, int precision, size_t order_bound, int group
     if (is_tc(resolve_arith(a, SFMM_M2L, Pb)))
         return fail(c, SFMM_UNSUPPORTED, "the tensor-core kernel runs one thread per translation");
     if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, SFMM_CUDA_ERROR, "cannot select device %d", c->device);
-    LaunchShape s = best_shape(a, Pb, group);
-    if (!s.acc) return fail(c, SFMM_INVALID_ARG, "no kernel runs %d threads per translation at order %d", group, Pb);
+    LaunchShape s[3];
+    for (int op = SFMM_M2M; op <= SFMM_L2L; ++op) {  // every operator at this order
+        s[op - SFMM_M2M] = best_shape(resolve_arith(a, op, Pb), Pb, group);
+        if (!s[op - SFMM_M2M].acc)
+            return fail(c, SFMM_INVALID_ARG, "no kernel runs %d threads per translation at order %d", group, Pb);
+    }
     std::lock_guard<std::mutex> lk2(c->setup_mtx);
-    c->shapes[std::make_pair((int)a, Pb)] = s;
+    for (int op = SFMM_M2M; op <= SFMM_L2L; ++op)
+        c->shapes[std::make_tuple(op, (int)resolve_arith(a, op, Pb), Pb)] = s[op - SFMM_M2M];
     return SFMM_OK;
 }
 
@@ -644,7 +648,7 @@ int sfmm_tune(sfmm_context *c, int op, int precision, size_t order_bound, size_t
         if (rate) *rate = ms > 0 ? 3.0 * (double)n / (ms * 1e-3) : 0.0;
         return SFMM_OK;
     }
-    const auto key = std::make_pair((int)a, Pb);
+    const auto key = std::make_tuple(op, (int)a, Pb);
     LaunchShape best;
     double best_rate = 0;
     // candidates: every group size that runs at this order, each with the

@@ -95,7 +95,9 @@ struct sfmm_context {
     sfmm::DevBuf d_eval;  // normalised expansions of the float-float L2P/M2P
     sfmm::HostBuf h_src, h_dst, h_meta, h_shift;
     cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
-    std::map<std::pair<int, int>, sfmm::LaunchShape> shapes;  // (arith, order bound) -> launch shape
+    // (op, arith, order bound) -> launch shape: operators tuned apart keep
+    // their own shapes at one order
+    std::map<std::tuple<int, int, int>, sfmm::LaunchShape> shapes;
     int *d_woff = nullptr, *d_hoff = nullptr;            // table offsets (shared by all arithmetics)
     int *d_woff8 = nullptr;                              // offsets of the 8-row padded swap blocks
     bool pageable_access = false;  // the GPU reads pageable host memory through the host page tables
@@ -131,6 +133,8 @@ const void *device_view(sfmm_context *c, const void *host);
 // tables and launch shape of (arithmetic, order bound) for op, so that a
 // launch makes no allocation (plans call this before a graph capture)
 int prepare_launch(sfmm_context *c, int op, Arith a, int Pbound, LaunchShape *shape = nullptr);
+// replace (or, with nullptr, drop) the cached launch shape of (op, arith, order bound)
+void set_shape(sfmm_context *c, std::tuple<int, int, int> key, const LaunchShape *s);
 // one validated translation launch on device pointers (translation i of the
 // batch is perm[i] when perm is given)
 // A work list (work, work_counter, nwork: see KParams) turns the launch into

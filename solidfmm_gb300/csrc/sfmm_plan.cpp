@@ -163,6 +163,80 @@ int record(sfmm_plan *p)
     return SFMM_OK;
 }
 
+// A segment's launch shape measured on the segment itself: its sources,
+// index arrays, orders and shifts and its stage's atomic mode, written into a
+// scratch copy of the target array (the plan's targets stay untouched).
+// Every candidate shape (each group size with its largest and smallest
+// full-occupancy tile, among CTAs of four warps or more and among all) runs
+// once to warm up and once timed.  *done stays false when the scratch
+// targets would take more than a quarter of the free device memory or
+// cannot be allocated: the caller then measures on synthetic data.
+int tune_segment(sfmm_context *c, const sfmm_plan *p, const Stage &s, const Segment &g, bool *done)
+{
+    *done = false;
+    const Arith a = resolve_arith(s.a, s.op, g.bound);
+    const size_t bytes = s.dcount * s.dstride * (c->dtype == SFMM_F64 ? 8 : 4);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return SFMM_OK;
+    }
+    if (bytes == 0 || bytes > free_b / 4) return SFMM_OK;
+    void *dst = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaMalloc(&dst, bytes) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess) {
+        (void)cudaGetLastError();
+        if (dst) cudaFree(dst);
+        if (e0) cudaEventDestroy(e0);
+        return SFMM_OK;
+    }
+    const uint32_t *perm = p->d_perm + s.perm_off + g.off;
+    const auto key = std::make_tuple(s.op, (int)a, g.bound);
+    LaunchShape cands[12], best;
+    int ncand = 0;
+    for (int G : {4, 8, 32})
+        for (int min_threads : {128, 32})
+            for (bool small : {false, true}) {
+                const LaunchShape sh = best_shape(a, g.bound, G, small, min_threads);
+                bool seen = !sh.acc;
+                for (int k = 0; k < ncand && !seen; ++k) seen = cands[k].G == sh.G && cands[k].TS == sh.TS;
+                if (!seen) cands[ncand++] = sh;
+            }
+    float best_ms = 0;
+    int st = SFMM_OK;
+    cudaError_t e = cudaMemsetAsync(dst, 0, bytes, c->stream);
+    for (int ci = 0; ci < ncand && st == SFMM_OK && e == cudaSuccess; ++ci) {
+        set_shape(c, key, &cands[ci]);
+        for (int rep = 0; rep < 2 && st == SFMM_OK && e == cudaSuccess; ++rep) {
+            if (rep == 1) e = cudaEventRecord(e0, c->stream);
+            st = run_batch(c, c->stream, s.op, s.a, g.bound, (long long)g.cnt, s.src, (long long)s.sstride,
+                           (long long)s.scount, s.sidx, dst, (long long)s.dstride, (long long)s.dcount, s.tidx,
+                           s.pin, s.pout, s.shift, perm, s.flags, (long long)s.n);
+            if (rep == 1 && e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+        }
+        float ms = 0;
+        if (st == SFMM_OK && e == cudaSuccess && (e = cudaEventSynchronize(e1)) == cudaSuccess)
+            e = cudaEventElapsedTime(&ms, e0, e1);
+        if (st == SFMM_OK && e == cudaSuccess && (!best.acc || ms < best_ms)) {
+            best = cands[ci];
+            best_ms = ms;
+        }
+    }
+    cudaFree(dst);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    set_shape(c, key, best.acc ? &best : nullptr);
+    if (st != SFMM_OK) return st;
+    if (e != cudaSuccess) return cuda_fail(c, e, "plan: tuning a segment");
+    if (best.acc) {
+        std::lock_guard<std::mutex> lk(c->setup_mtx);
+        c->tuned.insert(std::make_tuple(s.op, (int)a, g.bound));
+        *done = true;
+    }
+    return SFMM_OK;
+}
+
 // Tiles of TS translations over order-sorted segments, largest order bound
 // first.
 void build_work(const std::vector<Segment> &segs, int TS, std::vector<uint2> &work)
@@ -442,9 +516,13 @@ int sfmm_plan_finalize(sfmm_plan *p)
                     have = c->tuned.count(key) != 0;
                 }
                 if (have) continue;
-                const size_t cnt = s.fused ? s.n : g.cnt;
-                int st = sfmm_tune(c, s.op, s.precision, (size_t)bound,
-                                   std::min<size_t>(std::max<size_t>(cnt, 4096), 65536), nullptr, nullptr);
+                bool done = false;
+                int st = tune_segment(c, p, s, g, &done);
+                if (st) return st;
+                if (done) continue;
+                const size_t cnt = s.fused ? s.n : g.cnt;  // too large a target array: synthetic data
+                st = sfmm_tune(c, s.op, s.precision, (size_t)bound,
+                               std::min<size_t>(std::max<size_t>(cnt, 4096), 65536), nullptr, nullptr);
                 if (st) return st;
             }
     std::vector<uint2> work;

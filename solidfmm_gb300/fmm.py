@@ -141,7 +141,7 @@ class UniformFMM:
     index order) with their charges; ``run`` returns nothing and leaves the
     results in ``M`` and ``L`` (all levels, ``offsets`` per level)."""
 
-    def __init__(self, ctx, depth: int, precision: int, device):
+    def __init__(self, ctx, depth: int, precision: int, device, tune: bool = False):
         import torch
 
         from . import _native
@@ -170,6 +170,8 @@ class UniformFMM:
             self._keep += [order, si, ti, sh]
             self.plan.add(st.op, precision, n, src, S, nbox, dst, S, nbox, order, order, sh, src_index=si,
                           dst_index=ti, repeat=st.repeat)
+        if tune:  # launch shapes measured per (operator, order bound) at finalize
+            self.plan.options(tune=True)
         self.plan.finalize()
 
     @property
