@@ -87,7 +87,8 @@ typedef enum {
 /* flags for the batch calls */
 enum {
     SFMM_TARGETS_UNIQUE = 0,   /* no two translations of the batch share a target */
-    SFMM_TARGETS_REPEAT = 1    /* targets may repeat: accumulate with atomics */
+    SFMM_TARGETS_REPEAT = 1,   /* targets may repeat: accumulate with atomics */
+    SFMM_TARGETS_ON_DEVICE = 2 /* sfmm_translate_host_packed: dst is device memory (see there) */
 };
 
 typedef struct sfmm_context sfmm_context;
@@ -141,7 +142,15 @@ int sfmm_device_status(sfmm_context *ctx, int *flags);
  * in sfmm_translate_device.  Copies in, translates, copies the updated
  * targets back and synchronises before returning.  Batches without index
  * arrays are pipelined in chunks over three streams so that host-to-device
- * copies, kernels and device-to-host copies overlap. */
+ * copies, kernels and device-to-host copies overlap.
+ * With SFMM_TARGETS_ON_DEVICE in flags, dst (dst_count expansions at
+ * dst_stride) is device memory that keeps the results across calls: the
+ * kernel reads the host sources where they lie (they must be
+ * device-accessible: pinned, or any host memory on a GPU that walks the host
+ * page tables, else SFMM_UNSUPPORTED) and accumulates into the device
+ * targets (atomics with SFMM_TARGETS_REPEAT), so the host link carries the
+ * sources and the batch metadata only -- 2.2 KB per translation at P=16
+ * instead of 6.5 KB.  Synchronises before returning. */
 int sfmm_translate_host_packed(sfmm_context *ctx, int op, int precision, size_t n,
                                const void *src, size_t src_stride, size_t src_count, const uint32_t *src_index,
                                void *dst, size_t dst_stride, size_t dst_count, const uint32_t *dst_index,

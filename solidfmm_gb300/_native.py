@@ -16,7 +16,7 @@ from . import build as _build
 F32, F64 = 0, 1
 M2M, M2L, L2L = 0, 1, 2
 PLAIN, SPLIT, SPLIT_FF, TC_TF32, TC_BF16, TC_BF16X6 = 0, 1, 2, 3, 4, 5
-TARGETS_UNIQUE, TARGETS_REPEAT = 0, 1
+TARGETS_UNIQUE, TARGETS_REPEAT, TARGETS_ON_DEVICE = 0, 1, 2
 PLAN_FUSED, PLAN_TUNE = 1, 2
 OPS = {"m2m": M2M, "m2l": M2L, "l2l": L2L}
 
@@ -213,7 +213,10 @@ class Context:
         return v.value
 
     def translate_host_packed(self, op, precision, src, dst, p_in, p_out, shift, src_index=None, dst_index=None,
-                              repeat=False):
+                              repeat=False, targets_on_device=False):
+        """sfmm_translate_host_packed: host sources and metadata; host targets
+        updated in place, or (targets_on_device) a device tensor of targets
+        that keeps the results across calls."""
         op = OPS.get(op, op)
         n = len(p_in)
         p_in = np.ascontiguousarray(p_in, np.uint32)
@@ -224,7 +227,7 @@ class Context:
         self._check(self.L.sfmm_translate_host_packed(
             self.h, op, precision, n, _ptr(src), src.shape[-1], src.shape[0], _ptr(si), _ptr(dst), dst.shape[-1],
             dst.shape[0], _ptr(ti), _ptr(p_in), _ptr(p_out), _ptr(shift),
-            TARGETS_REPEAT if repeat else TARGETS_UNIQUE))
+            (TARGETS_REPEAT if repeat else TARGETS_UNIQUE) | (TARGETS_ON_DEVICE if targets_on_device else 0)))
 
     def bucket(self, n, p_in, p_out, order):
         self._check(self.L.sfmm_bucket_by_order(self.h, n, _ptr(p_in), _ptr(p_out), _ptr(order)))

@@ -60,6 +60,34 @@ int sfmm_translate_host_packed(sfmm_context *c, int op, int precision, size_t n,
     for (int k = 0; k < 3; ++k)
         if (!c->pipe[k] && (e = cudaStreamCreateWithFlags(&c->pipe[k], cudaStreamNonBlocking)) != cudaSuccess)
             return cuda_fail(c, e, "stream create");
+    if (flags & SFMM_TARGETS_ON_DEVICE) {
+        // device-resident targets: the kernel streams the host sources over
+        // the link and accumulates in device memory (no target traffic on it)
+        const void *vs = device_view(c, src);
+        if (!vs) return fail(c, SFMM_UNSUPPORTED, "device targets need device-accessible host sources");
+        const size_t nm = n * (2 + (src_index ? 1 : 0) + (dst_index ? 1 : 0));
+        if ((e = c->d_meta[0].ensure(nm * sizeof(uint32_t))) != cudaSuccess ||
+            (e = c->d_shift[0].ensure(n * 3 * sizeof(double))) != cudaSuccess)
+            return cuda_fail(c, e, "device buffers");
+        uint32_t *dm = (uint32_t *)c->d_meta[0].p;
+        uint32_t *dsi = src_index ? dm + 2 * n : nullptr;
+        uint32_t *dti = dst_index ? dm + (src_index ? 3 : 2) * n : nullptr;
+        double *dsh = (double *)c->d_shift[0].p;
+        cudaStream_t s = c->pipe[0];
+        if ((e = cudaMemcpyAsync(dm, p_in, n * 4, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(dm + n, p_out, n * 4, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(dsh, shift, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s)) ||
+            (dsi && (e = cudaMemcpyAsync(dsi, src_index, n * 4, cudaMemcpyHostToDevice, s))) ||
+            (dti && (e = cudaMemcpyAsync(dti, dst_index, n * 4, cudaMemcpyHostToDevice, s))))
+            return cuda_fail(c, e, "host-to-device copy");
+        // the host-memory instance (no L2 prefetch: the sources are on the host)
+        st = run_batch(c, s, op, a, (int)pmax, (long long)n, vs, (long long)src_stride, (long long)src_count, dsi,
+                       dst, (long long)dst_stride, (long long)dst_count, dti, dm, dm + n, dsh, nullptr,
+                       flags & ~SFMM_TARGETS_ON_DEVICE, -1, nullptr, nullptr, false);
+        if (st) return st;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "synchronise");
+        return SFMM_OK;
+    }
     const bool pipelined = !src_index && !dst_index;
     // Zero-copy: when the caller's arrays are device-accessible (pinned host
     // memory, or any host memory where the GPU walks the host page tables, as

@@ -520,3 +520,49 @@ def test_host_packed_fp32(native, oracle, memory):
                                   repeat=repeat)
         err = rel_err(dst.astype(np.float64) - start, ref - start, norm_weights(P, "L"))
         assert err < 2e-5, (repeat, err)
+
+
+@pytest.mark.parametrize("indices", [False, True], ids=["contiguous", "indexed"])
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
+def test_host_packed_device_targets(native, ctx64, indices, pinned):
+    """SFMM_TARGETS_ON_DEVICE: host sources read over the link, targets kept in
+    device memory across calls: the same sums as sfmm_translate_device on the
+    same batch (bit-identical without repeats; the repeating case accumulates
+    with atomics)."""
+    import torch
+
+    P, n = 10, 3000
+    S = P * (P + 1)
+    rng = np.random.default_rng(21 + indices + 2 * pinned)
+    nsrc = 700 if indices else n
+    src = rng.normal(size=(nsrc, S))
+    sidx = rng.integers(0, nsrc, n).astype(np.uint32) if indices else None
+    tidx = rng.permutation(n).astype(np.uint32) if indices else None
+    pin = rng.integers(1, P + 1, n).astype(np.uint32)
+    pout = rng.integers(1, P + 1, n).astype(np.uint32)
+    d = rng.normal(size=(n, 3))
+    xyz = d / np.linalg.norm(d, axis=1, keepdims=True) * 3.0
+    dev = torch.device("cuda", 0)
+    hsrc = torch.from_numpy(src).pin_memory() if pinned else src
+    got = torch.zeros(n, S, dtype=torch.float64, device=dev)
+    for _ in range(2):  # accumulates across calls
+        ctx64.translate_host_packed("m2l", 1, hsrc, got, pin, pout, xyz, src_index=sidx, dst_index=tidx,
+                                    targets_on_device=True)
+    want = torch.zeros(n, S, dtype=torch.float64, device=dev)
+    t = lambda a: None if a is None else torch.as_tensor(a.astype(np.int32), device=dev)  # noqa: E731
+    for _ in range(2):
+        ctx64.translate_device("m2l", 1, n, torch.as_tensor(src, device=dev), S, nsrc, want, S, n, t(pin), t(pout),
+                               torch.as_tensor(xyz, device=dev), src_index=t(sidx), dst_index=t(tidx), order_bound=P)
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)
+    # repeated targets: atomics in device memory
+    rep_t = (np.arange(n) % 97).astype(np.uint32)
+    got_r = torch.zeros(97, S, dtype=torch.float64, device=dev)
+    ctx64.translate_host_packed("m2l", 1, hsrc, got_r, pin, pout, xyz, src_index=sidx, dst_index=rep_t,
+                                repeat=True, targets_on_device=True)
+    want_r = torch.zeros(97, S, dtype=torch.float64, device=dev)
+    ctx64.translate_device("m2l", 1, n, torch.as_tensor(src, device=dev), S, nsrc, want_r, S, 97, t(pin), t(pout),
+                           torch.as_tensor(xyz, device=dev), src_index=t(sidx), dst_index=t(rep_t), repeat=True,
+                           order_bound=P)
+    torch.cuda.synchronize()
+    assert float((got_r - want_r).abs().max()) <= 1e-12 * float(want_r.abs().max())
