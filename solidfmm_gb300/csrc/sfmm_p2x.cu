@@ -605,7 +605,14 @@ __device__ __forceinline__ int exp_of(float x)
     const int e = (int)((__float_as_uint(x) >> 23) & 0xffu);
     return e ? e - 127 : -(1 << 20);
 }
-__device__ __forceinline__ ff ff_of_scaled(double x, int sh) { return ff_from_d_scaled(x, sh); }
+// x 2^sh as float-float; zero and subnormal x give 0 whatever the shift (the
+// block exponent of a degree of tiny coefficients can make sh large enough
+// for ff_from_d_scaled's range test to miss them)
+__device__ __forceinline__ ff ff_of_scaled(double x, int sh)
+{
+    if ((((unsigned)__double2hiint(x) >> 20) & 0x7ffu) == 0u) return ff{0.f, 0.f};
+    return ff_from_d_scaled(x, sh);
+}
 __device__ __forceinline__ ff ff_of_scaled(float x, int sh) { return ff{ldexp2(x, max(-252, min(252, sh))), 0.f}; }
 
 template <class In>
@@ -623,8 +630,7 @@ __global__ void k_eval_prep(int kind, int P, long long nexp, const In *__restric
         const int se = kind ? kP2xTab.se[t0 + m] : -kP2xTab.se[t0 + m];
         s = max(s, max(exp_of(e[n * (n + 1) + m]), exp_of(e[(n + 1) * (n + 1) + m])) + se);
     }
-    if (s < -(1 << 19)) s = 0;  // an all-zero degree
-    sdeg[i] = s;
+    sdeg[i] = s;  // an all-zero degree keeps -2^20: it never sets a point's scale
     float4 *o = Mout + b * (P * (P + 1) / 2) + t0;
     for (int m = 0; m <= n; ++m) {
         const int se = kind ? kP2xTab.se[t0 + m] : -kP2xTab.se[t0 + m];
@@ -687,6 +693,11 @@ __global__ void __launch_bounds__(128) k_eval_ff(int kind, int P, long long npts
     const float4 *Mb = M + b * (P * (P + 1) / 2);
     const int *sb = sdeg + b * P;
     const bool want_grad = grad != nullptr && kind == 0;
+    // the sums run at the scale 2^-B of the largest degree and return to
+    // their own in FP64, so results beyond the FP32 range keep their digits
+    int B = -(1 << 29);
+    for (int n = 0; n < P; ++n) B = max(B, kind == 0 ? sb[n] + n * sh : sb[n] - (n + 1) * sh);
+    if (B < -(1 << 19)) B = 0;  // all coefficients zero
     // v^(2^i), i < 5: every v^m (m < 32) is a product of at most five of
     // them, so its rounding error grows with log m rather than with m
     cpx_ff v2i[5];
@@ -713,12 +724,12 @@ __global__ void __launch_bounds__(128) k_eval_ff(int kind, int P, long long npts
                 x2 = x1;
                 x1 = xn;
             }
-            const int ex = kind == 0 ? sb[n] + n * sh : sb[n] - (n + 1) * sh;
+            const int ex = (kind == 0 ? sb[n] + n * sh : sb[n] - (n + 1) * sh) - B;
             const cpx_ff e = eval_coef(Mb, n, m, ex);
             const ff t = ff_fms2(e.r, x1.r, ff{-e.i.hi, -e.i.lo}, x1.i);  // e_re X_re + e_im X_im
             ffacc_add(cphi, ff{t.hi * wm, t.lo * wm});
             if (want_grad && n + 1 < P) {
-                const int k1 = n + 1, ix = n * (n + 1) / 2 + m, ex1 = sb[k1] + k1 * sh;
+                const int k1 = n + 1, ix = n * (n + 1) / 2 + m, ex1 = sb[k1] + k1 * sh - B;
                 const cpx_ff ez = eval_coef(Mb, k1, m, ex1);
                 const ff tz = ff_fms2(ez.r, x1.r, ff{-ez.i.hi, -ez.i.lo}, x1.i);
                 ffacc_madd(cgz, ff_tab(kP2xTab.cz, ix), ff{tz.hi * wm, tz.lo * wm});
@@ -746,9 +757,9 @@ __global__ void __launch_bounds__(128) k_eval_ff(int kind, int P, long long npts
             gz = ff_add(gz, ff{cgz.hi, cgz.lo});
         }
     }
-    pot[j] += (double)phi.hi + (double)phi.lo;
+    pot[j] += ldexp((double)phi.hi + (double)phi.lo, B);
     if (want_grad) {
-        const double ir = ldexp(1.0, -sh);
+        const double ir = ldexp(1.0, B - sh);
         grad[3 * j] += ((double)gx.hi + (double)gx.lo) * ir;
         grad[3 * j + 1] += ((double)gy.hi + (double)gy.lo) * ir;
         grad[3 * j + 2] += ((double)gz.hi + (double)gz.lo) * ir;

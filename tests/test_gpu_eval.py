@@ -287,3 +287,24 @@ def test_l2p_at_the_centre(native, oracle, P):
     assert pot.item() == pytest.approx(L[0, 0], rel=1e-14, abs=0)
     ref = _grad_ref(oracle, L[0], P, np.zeros(3))
     assert np.max(np.abs(grad.cpu().numpy()[0] - ref)) <= 1e-14 * max(np.max(np.abs(ref)), 1e-300)
+
+
+def test_eval_tiny_coefficients_with_zeros(native, oracle):
+    """A local expansion scaled to ~1e-280 with exact zeros among its
+    coefficients: the zeros stay zero and the potential scales exactly."""
+    import torch
+
+    P = 8
+    rng = np.random.default_rng(12)
+    L = rng.normal(size=(1, P * (P + 1)))
+    L[0, ::3] = 0.0
+    pts = rng.normal(size=(20, 3)) * 0.3
+    ref = _pot(oracle, 0, L[0], P, pts, np.zeros(3))
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    pot = torch.zeros(20, dtype=torch.float64, device=dev)
+    ctx.evaluate(0, 20, torch.as_tensor(pts, device=dev), torch.as_tensor(L * 1e-280, device=dev), P * (P + 1), 1,
+                 torch.zeros(1, 3, dtype=torch.float64, device=dev), pot, box=torch.zeros(20, dtype=torch.int32, device=dev))
+    torch.cuda.synchronize()
+    got = pot.cpu().numpy() * 1e280
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
