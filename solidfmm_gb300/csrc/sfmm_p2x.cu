@@ -267,6 +267,26 @@ __device__ __forceinline__ void ffacc_add(ffacc &a, ff x)
     a.lo = __fadd_rn(a.lo, __fadd_rn(e, x.lo));
 }
 
+// binary exponent of x (x = f 2^e, f in [1, 2)); zero and subnormals give a
+// value below every other
+__device__ __forceinline__ int exp_of(double x)
+{
+    const int e = (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu);
+    return e ? e - 1023 : -(1 << 20);
+}
+__device__ __forceinline__ int exp_of(float x)
+{
+    const int e = (int)((__float_as_uint(x) >> 23) & 0xffu);
+    return e ? e - 127 : -(1 << 20);
+}
+
+// exponent of the largest component of (x, y, z): |x - c| lies in
+// [2^e, 2^(e+2)) (sqrt(3) 2^(e+1) < 2^(e+2)); -2^20 for the zero vector
+__device__ __forceinline__ int max_exp3(double x, double y, double z)
+{
+    return max(exp_of(x), max(exp_of(y), exp_of(z)));
+}
+
 // A lane's two columns as one run of P + 1 harmonics: column m1 at t < len1
 // (t = n - m1), then column m2 at t = len1 + n - m2.  X starts at each
 // diagonal (dg1, dg2) and follows the recurrence; the values of the window
@@ -339,24 +359,21 @@ __global__ void __launch_bounds__(128) k_p2x_ff(int kind, int P, long long nexp,
     }
     // rho = 2^sc: the largest (P2M) or smallest (P2L) distance of the
     // expansion's charges rounded to a power of two, up (P2M) or down (P2L)
-    float ext = kind == 0 ? 0.f : __int_as_float(0x7f800000);
+    // from the components' exponents, so any double scale works: rho =
+    // 2^(e+2) over the largest component's e (P2M: |x'| < 1) or 2^e over the
+    // smallest of the charges' largest components (P2L: |x'| >= 1)
+    const int kNone = -(1 << 20);
+    int ext = kind == 0 ? kNone : (1 << 20);
     for (long long it = l; it < cnt; it += LP) {
         const double *pp = pos + 3 * (kb + it);
-        const float dx = (float)(pp[0] - cx), dy = (float)(pp[1] - cy), dz = (float)(pp[2] - cz);
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        ext = kind == 0 ? fmaxf(ext, r2) : fminf(ext, r2);
+        const int e3 = max_exp3(pp[0] - cx, pp[1] - cy, pp[2] - cz);
+        if (e3 != kNone) ext = kind == 0 ? max(ext, e3) : min(ext, e3);
     }
     for (int d = LP / 2; d > 0; d >>= 1) {
-        const float o = __shfl_xor_sync(0xffffffffu, ext, d, LP);
-        ext = kind == 0 ? fmaxf(ext, o) : fminf(ext, o);
+        const int o = __shfl_xor_sync(0xffffffffu, ext, d, LP);
+        ext = kind == 0 ? max(ext, o) : min(ext, o);
     }
-    int sh = 0;  // log2 rho
-    if (ext > 0.f && ext < __int_as_float(0x7f800000)) {
-        int E;
-        frexpf(ext, &E);  // ext = f 2^E, f in [1/2, 1)
-        sh = kind == 0 ? (E + 1) >> 1 : (E - 1) >> 1;  // rho^2 >= ext (P2M), rho^2 <= ext / 2 (P2L)
-        sh = max(-100, min(100, sh));
-    }
+    const int sh = ext == kNone || ext == (1 << 20) ? 0 : (kind == 0 ? ext + 2 : ext);  // log2 rho
 
     ffacc ar[NT], ai[NT];
 #pragma unroll
@@ -593,18 +610,6 @@ __global__ void k_eval(int kind, int P, long long npts, const double *__restrict
 // coefficients v, v+1, v-1 as k_eval does with R_k^v, each pairing weighted
 // by sig(k+1, v')/sig(k, v), the sum divided by rho.
 
-// binary exponent of x (x = f 2^e, f in [1, 2)); zero and subnormals give a
-// value below every other
-__device__ __forceinline__ int exp_of(double x)
-{
-    const int e = (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu);
-    return e ? e - 1023 : -(1 << 20);
-}
-__device__ __forceinline__ int exp_of(float x)
-{
-    const int e = (int)((__float_as_uint(x) >> 23) & 0xffu);
-    return e ? e - 127 : -(1 << 20);
-}
 // x 2^sh as float-float; zero and subnormal x give 0 whatever the shift (the
 // block exponent of a degree of tiny coefficients can make sh large enough
 // for ff_from_d_scaled's range test to miss them)
@@ -667,14 +672,10 @@ __global__ void __launch_bounds__(128) k_eval_ff(int kind, int P, long long npts
     const long long b = box ? (long long)box[j] : j;
     const double dx = pos[3 * j] - centre[3 * b], dy = pos[3 * j + 1] - centre[3 * b + 1],
                  dz = pos[3 * j + 2] - centre[3 * b + 2];
-    // rho = 2^sh: rho^2 >= |x - c|^2 (L2P) or rho^2 <= |x - c|^2 / 2 (M2P)
-    const float r2f = (float)(dx * dx + dy * dy + dz * dz);
-    int sh = 0;
-    if (r2f > 0.f && r2f < __int_as_float(0x7f800000)) {
-        int Ex;
-        frexpf(r2f, &Ex);
-        sh = max(-100, min(100, kind == 0 ? (Ex + 1) >> 1 : (Ex - 1) >> 1));
-    }
+    // rho = 2^sh from the largest component's exponent e: 2^(e+2) > |x - c|
+    // (L2P), 2^e <= |x - c| (M2P); any double scale
+    const int e3 = max_exp3(dx, dy, dz);
+    const int sh = e3 == -(1 << 20) ? 0 : (kind == 0 ? e3 + 2 : e3);
     const ff x = ff_from_d_scaled(dx, -sh), y = ff_from_d_scaled(dy, -sh), z = ff_from_d_scaled(dz, -sh);
     const ff r2 = ff_add(ff_add(ff_mul(x, x), ff_mul(y, y)), ff_mul(z, z));
     ff zeta, eta, w0{1.f, 0.f};

@@ -308,3 +308,34 @@ def test_eval_tiny_coefficients_with_zeros(native, oracle):
     torch.cuda.synchronize()
     got = pot.cpu().numpy() * 1e280
     assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("kind", [0, 1], ids=["l2p", "m2p"])
+@pytest.mark.parametrize("scale", [1e-25, 1e20])
+def test_eval_scales_beyond_fp32_range(native, oracle, kind, scale):
+    """Geometry scaled so that |x - c|^2 leaves the FP32 range."""
+    import torch
+
+    P = 10
+    rng = np.random.default_rng(77 + kind)
+    q = rng.choice([-1.0, 1.0], size=(2, 12))
+    d = rng.normal(size=(2, 12, 3))
+    src = d / np.linalg.norm(d, axis=2, keepdims=True) * 0.4
+    if kind == 0:
+        src = src + np.array([3.0, -1.0, 2.0])
+    centres = np.array([[0.0, 0.0, 0.0], [0.5, 0.2, -0.1]])
+    E = oracle.p2m(P, q, (src + centres[:, None, :]) * scale, centres * scale, singular=(kind == 0))
+    u = rng.normal(size=(40, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    box = np.repeat(np.arange(2), 20).astype(np.uint32)
+    pts = (u * (0.3 if kind == 0 else 3.0) + centres[box]) * scale
+    ref = np.concatenate([_pot(oracle, kind, E[b], P, pts[box == b], centres[b] * scale) for b in range(2)])
+    scl = np.concatenate([_pot_abs(oracle, kind, E[b], P, pts[box == b], centres[b] * scale) for b in range(2)])
+    dev = torch.device("cuda", 0)
+    ctx = native.Context(P, "f64")
+    pot = torch.zeros(40, dtype=torch.float64, device=dev)
+    ctx.evaluate(kind, 40, torch.as_tensor(pts, device=dev), torch.as_tensor(E, device=dev), P * (P + 1), 2,
+                 torch.as_tensor(centres * scale, device=dev), pot,
+                 box=torch.as_tensor(box.astype(np.int32), device=dev))
+    torch.cuda.synchronize()
+    assert np.max(np.abs(pot.cpu().numpy() - ref) / scl) <= TOL_EVAL

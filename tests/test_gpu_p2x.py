@@ -175,3 +175,16 @@ def test_p2m_charge_at_the_centre(native, oracle, P):
     got = run_p2x(native, P, 0, q, pos, cen)
     assert got[0, 0] == 2.5 and np.all(got[0, 1:] == 0)
     assert p2x_err(got, ref, P, 0, q, pos, cen) < TOL_ABS
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("radius", [1e-25, 1e20])
+def test_scales_beyond_fp32_range(native, oracle, kind, radius):
+    """|x - c|^2 outside the FP32 range: the scale comes from the doubles'
+    exponents, so the float-float columns still see |x'| near 1."""
+    P = 12
+    rng = np.random.default_rng(31)
+    q, pos, cen = charges(rng, 8, 24, kind, radius=radius)
+    ref = oracle.p2m(P, q, pos, cen, singular=bool(kind))
+    got = run_p2x(native, P, kind, q, pos, cen)
+    assert p2x_err(got, ref, P, kind, q, pos, cen) < TOL_ABS
