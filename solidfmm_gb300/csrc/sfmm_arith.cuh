@@ -141,6 +141,14 @@ __device__ __forceinline__ ff ff_from_d_scaled(double x, int sh)
 // double -> float-float without FP64 instructions
 __device__ __forceinline__ ff ff_from_d_int(double x) { return ff_from_d_scaled(x, 0); }
 
+// ff_from_d_scaled for shifts of any size: zero and subnormal x give 0
+// (above a shift of 872 the range test alone would miss them)
+__device__ __forceinline__ ff ff_from_d_scaled0(double x, int sh)
+{
+    if ((((unsigned)__double2hiint(x) >> 20) & 0x7ffu) == 0u) return ff{0.f, 0.f};
+    return ff_from_d_scaled(x, sh);
+}
+
 // float -> double by re-biasing the exponent (exact); zero included, other
 // non-normal values take the conversion instruction.
 __device__ __forceinline__ double d_from_f_int(float f)
@@ -151,6 +159,84 @@ __device__ __forceinline__ double d_from_f_int(float f)
     if (ex == 0u || ex == 0xffu) return (double)f;
     const unsigned hi = (w & 0x80000000u) | ((ex + 896u) << 20) | ((w & 0x7fffffu) >> 3);
     return __hiloint2double((int)hi, (int)(w << 29));
+}
+
+// binary exponent of x (x = f 2^e, f in [1, 2)); zero and subnormals give a
+// value below every other
+__device__ __forceinline__ int exp_of(double x)
+{
+    const int e = (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu);
+    return e ? e - 1023 : -(1 << 20);
+}
+__device__ __forceinline__ int exp_of(float x)
+{
+    const int e = (int)((__float_as_uint(x) >> 23) & 0xffu);
+    return e ? e - 127 : -(1 << 20);
+}
+
+// x 2^e through the exponent field (exact): zero and subnormal x give zero,
+// results beyond the normal range zero or infinity
+__device__ __forceinline__ float f_scaled(float x, int e)
+{
+    const unsigned w = __float_as_uint(x);
+    const int ex = (int)((w >> 23) & 0xffu);
+    if (ex == 0 || ex == 0xff) return ex ? x : __uint_as_float(w & 0x80000000u);
+    const int ne = ex + e;
+    if (ne <= 0) return __uint_as_float(w & 0x80000000u);
+    if (ne >= 0xff) return __uint_as_float((w & 0x80000000u) | 0x7f800000u);
+    return __uint_as_float((w & 0x807fffffu) | ((unsigned)ne << 23));
+}
+
+// double x 2^e through the exponent field (exact): zero and subnormal x
+// give zero, results beyond the normal range zero or infinity
+__device__ __forceinline__ double d_scaled(double x, int e)
+{
+    const int h = __double2hiint(x);
+    const int ex = (int)(((unsigned)h >> 20) & 0x7ffu);
+    const int sg = h & (int)0x80000000u;
+    if (ex == 0) return __hiloint2double(sg, 0);
+    if (ex == 0x7ff) return x;
+    const int ne = ex + e;
+    if (ne <= 0) return __hiloint2double(sg, 0);
+    if (ne >= 0x7ff) return __hiloint2double(sg | 0x7ff00000, 0);
+    return __hiloint2double((h & (int)0x800fffffu) | (ne << 20), __double2loint(x));
+}
+
+// d_from_f_scaled for the rare inputs: zero, subnormal f (normalised
+// first), infinity and NaN, and results beyond the double range (zero below,
+// infinity above)
+__device__ __forceinline__ double d_from_f_scaled_rare(float f, int e)
+{
+    unsigned w = __float_as_uint(f);
+    int ex = (int)((w >> 23) & 0xffu);
+    const unsigned sg = w & 0x80000000u;
+    if (ex == 0) {
+        if ((w << 1) == 0u) return __hiloint2double((int)sg, 0);
+        w = __float_as_uint(f * 16777216.f);  // exact: 2^24
+        ex = (int)((w >> 23) & 0xffu);
+        e -= 24;
+    }
+    if (ex == 0xff) return (double)f;
+    const int ne = ex + 896 + e;
+    if (ne <= 0) return __hiloint2double((int)sg, 0);
+    if (ne >= 2047) return __hiloint2double((int)(sg | 0x7ff00000u), 0);
+    const unsigned hi = sg | ((unsigned)ne << 20) | ((w & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(w << 29));
+}
+
+// float -> double times 2^e by re-biasing the exponent (exact; d_from_f_int
+// with a shift): one range test for normal inputs with normal results, the
+// other cases out of line
+__device__ __forceinline__ double d_from_f_scaled(float f, int e)
+{
+    const unsigned w = __float_as_uint(f);
+    const int ex = (int)((w >> 23) & 0xffu);
+    const int ne = ex + 896 + e;
+    if (__builtin_expect((unsigned)(ex - 1) < 254u && (unsigned)(ne - 1) < 2046u, 1)) {
+        const unsigned hi = (w & 0x80000000u) | ((unsigned)ne << 20) | ((w & 0x7fffffu) >> 3);
+        return __hiloint2double((int)hi, (int)(w << 29));
+    }
+    return d_from_f_scaled_rare(f, e);
 }
 
 // float-float square root and reciprocal: one Newton step from the FP32

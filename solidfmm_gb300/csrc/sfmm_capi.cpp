@@ -311,6 +311,8 @@ int run_batch(sfmm_context *c, cudaStream_t stream, int op, Arith a, int Pbound,
     if (grid > tiles) grid = tiles;
     if (grid < 1) return fail(c, SFMM_CUDA_ERROR, "no launch shape runs order %d (G %d, %d translations per CTA)",
                               Pbound, s.G, s.TS);
+    if (a != Arith::F64 && s.spad > kDegreeTableSize)
+        return fail(c, SFMM_UNSUPPORTED, "buffer of %d slots above the FP32-range kernels' degree table", s.spad);
     if (wl) {  // the tile descriptor's two words after the meta arrays
         s.smem += 8;
         if (s.smem > 232448) return fail(c, SFMM_UNSUPPORTED, "work-list launch above the shared-memory limit");

@@ -267,18 +267,6 @@ __device__ __forceinline__ void ffacc_add(ffacc &a, ff x)
     a.lo = __fadd_rn(a.lo, __fadd_rn(e, x.lo));
 }
 
-// binary exponent of x (x = f 2^e, f in [1, 2)); zero and subnormals give a
-// value below every other
-__device__ __forceinline__ int exp_of(double x)
-{
-    const int e = (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu);
-    return e ? e - 1023 : -(1 << 20);
-}
-__device__ __forceinline__ int exp_of(float x)
-{
-    const int e = (int)((__float_as_uint(x) >> 23) & 0xffu);
-    return e ? e - 127 : -(1 << 20);
-}
 
 // exponent of the largest component of (x, y, z): |x - c| lies in
 // [2^e, 2^(e+2)) (sqrt(3) 2^(e+1) < 2^(e+2)); -2^20 for the zero vector
@@ -613,11 +601,7 @@ __global__ void k_eval(int kind, int P, long long npts, const double *__restrict
 // x 2^sh as float-float; zero and subnormal x give 0 whatever the shift (the
 // block exponent of a degree of tiny coefficients can make sh large enough
 // for ff_from_d_scaled's range test to miss them)
-__device__ __forceinline__ ff ff_of_scaled(double x, int sh)
-{
-    if ((((unsigned)__double2hiint(x) >> 20) & 0x7ffu) == 0u) return ff{0.f, 0.f};
-    return ff_from_d_scaled(x, sh);
-}
+__device__ __forceinline__ ff ff_of_scaled(double x, int sh) { return ff_from_d_scaled0(x, sh); }
 __device__ __forceinline__ ff ff_of_scaled(float x, int sh) { return ff{ldexp2(x, max(-252, min(252, sh))), 0.f}; }
 
 template <class In>

@@ -9,6 +9,10 @@ namespace sfmm {
 
 enum { OP_M2M = 0, OP_M2L = 1, OP_L2L = 2 };
 
+// buffer slots per translation covered by the FP32-range kernels' table of
+// coefficient degrees (every order up to 28 with its padding)
+constexpr int kDegreeTableSize = 1024;
+
 struct KParams {
     int op;
     int P;          // order bound of this batch: every p_in/p_out <= P

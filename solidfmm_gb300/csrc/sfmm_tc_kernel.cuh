@@ -191,14 +191,17 @@ __device__ __forceinline__ float tf32_rna(float x)
     return __uint_as_float(r);
 }
 
-// FP64 -> FP32 with integer operations (round half up; |x| < 2^-126 -> 0;
-// the FP64 pipe runs at 1/64 of the FP32 rate)
-__device__ __forceinline__ float f32_from_d(double x)
+// FP64 x 2^e -> FP32 with integer operations (round half up; results below
+// 2^-126, zero and subnormal x -> 0, above the FP32 range -> infinity; the
+// FP64 pipe runs at 1/64 of the FP32 rate)
+__device__ __forceinline__ float f32_from_d(double x, int e = 0)
 {
     const uint32_t hw = (uint32_t)__double2hiint(x), lw = (uint32_t)__double2loint(x);
-    const int ef = (int)((hw >> 20) & 0x7ffu) - 1023 + 127;
+    const int ed = (int)((hw >> 20) & 0x7ffu);
+    const int ef = ed - 1023 + 127 + e;
     uint32_t b = ((uint32_t)ef << 23) + (((hw & 0xfffffu) << 3) | (lw >> 29)) + ((lw >> 28) & 1u);
-    if (ef <= 0) b = 0;
+    if (ef <= 0 || ed == 0) b = 0;
+    if (ef >= 255) b = 0x7f800000u;
     return __uint_as_float(b | (hw & 0x80000000u));
 }
 
@@ -516,6 +519,22 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
             z = 1;
         }
         if (op == OP_L2L) pout = min(pin, pout);  // translations.cpp:412
+        // the translation's length scale lambda = 2^ks, |shift| / lambda in
+        // [2, 7): sources times lambda^-n (multipoles) or lambda^(n+1)
+        // (locals), results back, all exact in the conversions, so that the
+        // edge factors r^n and r^-(n+1) stay in range at any geometry scale
+        int ks = 0;
+        {
+            const int e3 = max(exp_of(x), max(exp_of(y), exp_of(z)));  // |shift| in [2^e3, sqrt(3) 2^(e3+1))
+            if (valid && !ident_p && e3 > -(1 << 19)) {
+                ks = e3 - 1;
+                x = d_scaled(x, -ks);
+                y = d_scaled(y, -ks);
+                z = d_scaled(z, -ks);
+            }
+        }
+        const int es = op == OP_L2L ? ks : -ks, es0 = op == OP_L2L ? ks : 0;   // source degree n: es n + es0
+        const int eo = op == OP_M2M ? ks : -ks, eo0 = op == OP_M2M ? 0 : -ks;  // output degree j: eo j + eo0
         // pointer mode: per-translation addresses (host solids the GPU reads in place)
         const double *sp = p.src_ptr ? reinterpret_cast<const double *>(p.src_ptr[si]) : src + (long long)si * p.sstride;
         double *dp = p.dst_ptr ? reinterpret_cast<double *>(p.dst_ptr[ti]) : dst + (long long)ti * p.dstride;
@@ -634,7 +653,8 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                     if (ln.on) {
                         const int e = ln.n * (ln.n + 1) / 2 + ln.m;
                         if constexpr (FF) {  // float-float edge, split without rounding to FP32
-                            const ff xr = ff_from_d_int(xr_n[jj]), xi = ff_from_d_int(xi_n[jj]);
+                            const int esh = es * ln.n + es0;
+                            const ff xr = ff_from_d_scaled0(xr_n[jj], esh), xi = ff_from_d_scaled0(xi_n[jj], esh);
                             const ff gg = A::mul(ff{RPW(0, ln.n), RPW(2, ln.n)}, ff{sEin[e], sEin[kNE + e]});
                             const ff gc = A::mul(gg, ff{PW(0, ln.m), PW(4, ln.m)});
                             const ff gs = A::mul(gg, ff{PW(1, ln.m), PW(5, ln.m)});
@@ -644,7 +664,8 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                             vi[jj] = yi.hi;
                             vi_lo[jj] = yi.lo;
                         } else {
-                            const float xr = tcd::f32_from_d(xr_n[jj]), xi = tcd::f32_from_d(xi_n[jj]);
+                            const int esh = es * ln.n + es0;
+                            const float xr = tcd::f32_from_d(xr_n[jj], esh), xi = tcd::f32_from_d(xi_n[jj], esh);
                             const float gg = RPW(0, ln.n) * sEin[e];
                             const float gc = gg * PW(0, ln.m), gs = gg * PW(1, ln.m);
                             vr[jj] = gc * xr - gs * xi;
@@ -803,13 +824,15 @@ __global__ void __launch_bounds__(kTcRows *NWG, 1) k_translate_tc(KParams p, TcT
                             const ff gs = A::mul(gg, ff{PW(1, ln.m), PW(5, ln.m)});
                             const ff xr{ur[jj], 0.f}, xi{ui[jj], 0.f};
                             const ff yr = A::dot2(gc, xr, gs, xi), yi = A::dot2(gc, xi, A::neg(gs), xr);
-                            orr = d_from_f_int(yr.hi) + d_from_f_int(yr.lo);
-                            oi = d_from_f_int(yi.hi) + d_from_f_int(yi.lo);
+                            const int esh = eo * ln.n + eo0;
+                            orr = d_from_f_scaled(yr.hi, esh) + d_from_f_scaled(yr.lo, esh);
+                            oi = d_from_f_scaled(yi.hi, esh) + d_from_f_scaled(yi.lo, esh);
                         } else {
                             const float gg = RPW(1, ln.n) * sEout[e];
                             const float gc = gg * PW(0, ln.m), gs = gg * PW(1, ln.m);
-                            orr = d_from_f_int(gc * ur[jj] + gs * ui[jj]);
-                            oi = d_from_f_int(gc * ui[jj] - gs * ur[jj]);
+                            const int esh = eo * ln.n + eo0;
+                            orr = d_from_f_scaled(gc * ur[jj] + gs * ui[jj], esh);
+                            oi = d_from_f_scaled(gc * ui[jj] - gs * ur[jj], esh);
                         }
                         double *pr = dp + ln.n * (ln.n + 1) + ln.m, *pi = dp + (ln.n + 1) * (ln.n + 1) + ln.m;
                         if (p.atomic) {

@@ -501,6 +501,36 @@ struct cff {
     ff c, s;
 };
 
+// Degree n of every coefficient index c below kDegreeTableSize (n(n+1) <= c
+// < (n+1)(n+2)): the FP32-range kernels scale each coefficient by a power of
+// two per degree in the gather and the target update, and one cached byte
+// load per coefficient issues fewer instructions than computing the degree.
+// Covers the buffers of every order those kernels run (up to 28: at most
+// 28 * 29 + 4 slots plus padding), checked on the host against
+// kDegreeTableSize.
+struct DegreeTable {
+    unsigned char d[kDegreeTableSize];
+};
+constexpr DegreeTable make_degree_table()
+{
+    DegreeTable t{};
+    int n = 0;
+    for (int c = 0; c < kDegreeTableSize; ++c) {
+        while ((n + 1) * (n + 2) <= c) ++n;
+        t.d[c] = (unsigned char)n;
+    }
+    return t;
+}
+__device__ const DegreeTable kDegree = make_degree_table();
+__device__ __forceinline__ int degree_at(int c) { return (int)__ldg(kDegree.d + c); }
+
+// source coefficient times 2^e in the arithmetic's storage type (exact)
+__device__ __forceinline__ ff src_scaled(double x, int e, const ff *) { return ff_from_d_scaled0(x, e); }
+__device__ __forceinline__ float src_scaled(float x, int e, const float *) { return f_scaled(x, e); }
+// FP64 sources of the FP32 kernel: scaled in FP64 first, so that sources
+// beyond the FP32 range come into it
+__device__ __forceinline__ float src_scaled(double x, int e, const float *) { return (float)d_scaled(x, e); }
+
 // Per-thread geometry of one translation: |shift|, its inverse and the
 // rotation factors.  FP64 for the FP64 and FP32 kernels; float-float for the
 // split kernels, which then execute no FP64 instruction here (GB300's FP64
@@ -582,6 +612,16 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
     // and the FP32 kernel 3.7% faster than 4 and 1, which the FP64 and
     // float-float kernels keep (1.5% and 0.7% slower with 8 and 4).
     constexpr bool kDeep = FIX || std::is_same<A, float>::value;
+    // FP32-range arithmetics run every translation at the length scale of
+    // its shift: lambda = 2^ks with |shift| / lambda in [2, 7), sources (and
+    // the shift) divided by lambda^n (multipoles) or lambda^-(n+1) (locals),
+    // results multiplied back -- the operators are homogeneous, and powers of
+    // two are exact, so only the range changes.  With r = |shift| / lambda in
+    // [2, 7) the edge factors (r^-(n+1) or r^n times the basis factors
+    // sqrt((n-m)!(n+m)!) or their inverses, up to 5e35 at order 28) stay
+    // inside the FP32 range at every geometry scale; shifts whose largest
+    // component lies in [2, 4) run unscaled
+    constexpr bool kScale = !std::is_same<A, double>::value;
     constexpr int kGatherUnroll = kDeep ? 8 : 4;
     constexpr int kAccUnroll = kDeep ? 4 : 1;
 
@@ -674,10 +714,20 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             z = 1;
         }
         if (op == OP_L2L) pout = min(pin, pout);  // output degrees >= P_in receive nothing (translations.cpp:412)
+        int ks = 0;
+        if constexpr (kScale) {
+            const int e3 = max(exp_of(x), max(exp_of(y), exp_of(z)));  // |shift| in [2^e3, sqrt(3) 2^(e3+1))
+            if (valid && !ident && e3 > -(1 << 19)) {
+                ks = e3 - 1;
+                x = d_scaled(x, -ks);
+                y = d_scaled(y, -ks);
+                z = d_scaled(z, -ks);
+            }
+        }
         if (q == 0) {
             m_sidx[slot] = valid ? si : 0;
             m_tidx[slot] = valid ? ti : 0;
-            m_pin[slot] = pin;
+            m_pin[slot] = (uint32_t)pin | ((uint32_t)(ks + 32768) << 16);  // order, and the scale above it
             m_pout[slot] = pout;
             m_id[slot] = ident_p;
         }
@@ -690,12 +740,20 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
         //    Sources and targets stream through with evict-first hints so the
         //    coefficient tables stay in the L1 left beside the buffers.
         for (int s = warp; s < TS; s += nwarps) {
-            const int ps = (int)m_pin[s];
+            const int ps = (int)(m_pin[s] & 0xffffu);
             const int cnt = ps * (ps + 1);
             const Src *sp = p.src_ptr ? reinterpret_cast<const Src *>(p.src_ptr[m_sidx[s]])
                                       : src + (long long)m_sidx[s] * p.sstride;
             S *bp = buf0 + (long long)s * p.spad;
-            if constexpr (HBM) {  // kGatherUnroll loads in flight per lane
+            if constexpr (kScale) {  // coefficient c of degree n times lambda^-n or lambda^(n+1)
+                const int ksg = (int)(m_pin[s] >> 16) - 32768;
+                const int es = op == OP_L2L ? ksg : -ksg;  // per degree
+                const int e0 = op == OP_L2L ? ksg : 0;
+#pragma unroll(kGatherUnroll)
+                for (int c = lane; c < p.spad; c += 32)
+                    AR::st(bp + c, c < cnt ? src_scaled(__ldcs(sp + c), es * degree_at(c) + e0, (const T *)nullptr)
+                                           : AR::zero());
+            } else if constexpr (HBM) {  // kGatherUnroll loads in flight per lane
 #pragma unroll(kGatherUnroll)
                 for (int c = lane; c < p.spad; c += 32)
                     AR::st(bp + c, c < cnt ? AR::from_src(__ldcs(sp + c)) : AR::zero());
@@ -820,8 +878,13 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
             const Src *sp = p.src_ptr ? reinterpret_cast<const Src *>(p.src_ptr[m_sidx[s]])
                                       : src + (long long)m_sidx[s] * p.sstride;
             Src *dp = p.dst_ptr ? reinterpret_cast<Src *>(p.dst_ptr[m_tidx[s]]) : dst + (long long)m_tidx[s] * p.dstride;
+            // back from the translation's length scale: output coefficient c of
+            // degree j times lambda^j (multipoles) or lambda^-(j+1) (locals)
+            const int ksa = (int)(m_pin[s] >> 16) - 32768;
+            const int eo = op == OP_M2M ? ksa : -ksa, eo0 = op == OP_M2M ? 0 : -ksa;
 #pragma unroll(kAccUnroll)
             for (int c = lane; c < cnt; c += 32) {
+                const int j = kScale ? degree_at(c) : 0;
                 if constexpr (AR::split) {
                     // hi and lo widen by exponent re-biasing; two FP64 additions
                     // (one FP64 addition after an integer-only hi + lo measured
@@ -829,7 +892,8 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
                     double v = p.atomic ? 0.0 : (double)__ldcs(dp + c);
                     if (c < po * (po + 1)) {
                         const T t = AR::ld(bp + c);
-                        const double hd = d_from_f_int(t.hi), lo = d_from_f_int(t.lo);
+                        const int e = eo * j + eo0;
+                        const double hd = d_from_f_scaled(t.hi, e), lo = d_from_f_scaled(t.lo, e);
                         v = p.atomic ? hd + lo : (v + hd) + lo;
                     }
                     if (c < pid * (pid + 1)) v += (double)__ldcs(sp + c);
@@ -837,7 +901,11 @@ __global__ void __launch_bounds__(256) k_translate(KParams p)
                     else __stcs(dp + c, (Src)v);
                 } else {
                     double v = 0;
-                    if (c < po * (po + 1)) v = AR::to_d(AR::ld(bp + c));
+                    if constexpr (kScale) {
+                        if (c < po * (po + 1)) v = d_from_f_scaled(AR::ld(bp + c), eo * j + eo0);
+                    } else if (c < po * (po + 1)) {
+                        v = AR::to_d(AR::ld(bp + c));
+                    }
                     if (c < pid * (pid + 1)) v += (double)__ldcs(sp + c);
                     if (p.atomic) atomicAdd(dp + c, (Src)v);
                     else __stcs(dp + c, (Src)((double)__ldcs(dp + c) + v));

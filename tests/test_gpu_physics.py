@@ -15,7 +15,7 @@ reference library was built (within 1e-9 relative of its printed error).
 import numpy as np
 import pytest
 
-from helpers import physics_errors, physics_gpu, physics_inputs, physics_reference
+from helpers import norm_weights, physics_errors, physics_gpu, physics_inputs, physics_reference, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -53,3 +53,53 @@ def test_physics_plain_matches_reference_double(ctx16, oracle, op):
         pytest.skip("reference library not built on this machine")
     pot, _ = physics_gpu(ctx16, op, 16, 0)
     assert abs(pot - ref[0]) <= 1e-9 * ref[0] + 1e-14, (pot, ref)
+
+
+def norm_weights_for(op, P):
+    return norm_weights(P, "M" if op == "m2m" else "L")
+
+
+SCALE_TOL = {0: 1e-12, 1: 1e-7, 2: 1e-11, 3: 4e-6, 5: 1.5e-6, 4: 2e-4}
+
+
+@pytest.mark.parametrize("op", ["m2l", "m2m", "l2l"])
+def test_every_mode_at_every_length_scale(ctx16, oracle, native, op):
+    """The same tree shape at length scales 1e-9 ... 1e9: translations are
+    homogeneous (multipole degree n scales as s^n, local degree n as
+    s^-(n+1)), so every precision mode keeps its accuracy at every scale,
+    although the coefficients span far more than the FP32 range.  Errors are
+    measured after bringing both results back to unit scale degree by degree
+    (the norms stay finite) in the orthonormal basis."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    P, n = 16, 48
+    S = P * (P + 1)
+    deg = np.array([k for k in range(P) for _ in range(2 * k + 2)], dtype=np.float64)
+    w = norm_weights_for(op, P)
+    for scale in (1e-9, 1e-4, 1e-2, 1.0, 1e2, 1e4, 1e9):
+        rng = np.random.default_rng(5)
+        q = rng.choice([-1.0, 1.0], size=(n, 12))
+        d = rng.normal(size=(n, 12, 3))
+        d /= np.linalg.norm(d, axis=2, keepdims=True)
+        if op == "l2l":  # locals of far charges
+            src = oracle.p2m(P, q, (d * 0.4 + np.array([3.0, 0.5, -1.0])) * scale, np.zeros((n, 3)), singular=True)
+        else:
+            src = oracle.p2m(P, q, d * 0.4 * rng.random((n, 12, 1)) * scale, np.zeros((n, 3)))
+        u = rng.normal(size=(n, 3))
+        xyz = u / np.linalg.norm(u, axis=1, keepdims=True) * (3.0 if op == "m2l" else 0.5) * scale
+        pin = np.full(n, P, np.uint32)
+        ref = np.zeros((n, S))
+        oracle.naive(op, src, pin, ref, pin, xyz)
+        # unit-scale weights per coefficient: s^-n for multipoles, s^(n+1) for locals
+        unit = np.exp(np.log(scale) * (-deg if op == "m2m" else deg + 1))
+        t_pin = torch.as_tensor(pin.astype(np.int32), device=dev)
+        t_src = torch.as_tensor(src, device=dev)
+        t_xyz = torch.as_tensor(xyz, device=dev)
+        for prec, tol in SCALE_TOL.items():
+            out = torch.zeros(n, S, dtype=torch.float64, device=dev)
+            ctx16.translate_device(op, prec, n, t_src, S, n, out, S, n, t_pin, t_pin, t_xyz, order_bound=P)
+            got = out.cpu().numpy()
+            assert np.isfinite(got).all(), (op, scale, prec)
+            err = rel_err(got * unit, ref * unit, w)
+            assert err <= tol, (op, scale, prec, err)
