@@ -85,6 +85,32 @@ def test_rotation_port_vs_formula_mixed_orders(oracle, op):
     assert rel_err(r - b["dst"], a - b["dst"]) < 1e-10
 
 
+@pytest.mark.parametrize("op", ["m2m", "m2l", "l2l"])
+def test_translations_are_homogeneous_in_length(oracle, op):
+    """Scaling every length by a power of two lambda scales multipole degree
+    n by lambda^n and local degree n by lambda^-(n+1), exactly: translating
+    the scaled sources by the scaled shift and scaling the result back gives
+    the unit-scale result.  The FP32-range kernels run every translation at
+    the length scale of its shift on this property."""
+    import inputs
+
+    rng = np.random.default_rng(7)
+    P = 12
+    b = inputs.make_batch(rng, op, P, P, 30, nq=8)
+    deg = np.array([k for k in range(P) for _ in range(2 * k + 2)], dtype=np.float64)
+    src_kind_m = op != "l2l"
+    out_kind_m = op == "m2m"
+    ref = np.zeros_like(b["dst"])
+    oracle.naive(op, b["src"], b["Pin"], ref, b["Pout"], b["xyz"])
+    for k in (-24, -3, 5, 24):  # the FP64 oracle's r^(n+k+1) stays in range
+        lam = 2.0 ** k
+        src = b["src"] * (lam ** deg if src_kind_m else lam ** -(deg + 1))
+        got = np.zeros_like(ref)
+        oracle.naive(op, src, b["Pin"], got, b["Pout"], b["xyz"] * lam)
+        got = got * (lam ** -deg if out_kind_m else lam ** (deg + 1))
+        assert rel_err(got, ref) < 1e-13, (op, k)
+
+
 def test_threaded_port_equals_serial(oracle):
     import inputs
 
