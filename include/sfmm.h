@@ -74,7 +74,12 @@ typedef enum { SFMM_M2M = 0, SFMM_M2L = 1, SFMM_L2L = 2 } sfmm_op;
  *           and float-float edge scaling: each MMA stage rounds about once
  *           in FP32.
  * The split and tensor-core modes need an SFMM_F64 context and orders <= 28
- * (FP32 exponent range of the orthogonal-basis scale factors). */
+ * (FP32 exponent range of the orthogonal-basis scale factors).  They, and
+ * PLAIN on an SFMM_F32 context, run every translation at the length scale
+ * of its own shift (sources and results rescaled by exact powers of two in
+ * the FP64 <-> FP32 conversions), so their error does not depend on the
+ * geometry's length scale; an SFMM_F32 context can only hold coefficients
+ * inside the FP32 range. */
 typedef enum {
     SFMM_PLAIN = 0,
     SFMM_SPLIT = 1,
