@@ -62,6 +62,53 @@ def norm_weights_for(op, P):
 SCALE_TOL = {0: 1e-12, 1: 1e-7, 2: 1e-11, 3: 4e-6, 5: 1.5e-6, 4: 2e-4}
 
 
+def _scaled_batch(oracle, op, P, n, scale):
+    """Sources of the tree shape at one length scale, their shifts, the FP64
+    oracle's translation and the per-coefficient factors back to unit scale
+    (s^-n for multipole results, s^(n+1) for local results)."""
+    rng = np.random.default_rng(5)
+    q = rng.choice([-1.0, 1.0], size=(n, 12))
+    d = rng.normal(size=(n, 12, 3))
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    if op == "l2l":  # locals of far charges
+        src = oracle.p2m(P, q, (d * 0.4 + np.array([3.0, 0.5, -1.0])) * scale, np.zeros((n, 3)), singular=True)
+    else:
+        src = oracle.p2m(P, q, d * 0.4 * rng.random((n, 12, 1)) * scale, np.zeros((n, 3)))
+    u = rng.normal(size=(n, 3))
+    xyz = u / np.linalg.norm(u, axis=1, keepdims=True) * (3.0 if op == "m2l" else 0.5) * scale
+    pin = np.full(n, P, np.uint32)
+    ref = np.zeros((n, P * (P + 1)))
+    oracle.naive(op, src, pin, ref, pin, xyz)
+    deg = np.array([k for k in range(P) for _ in range(2 * k + 2)], dtype=np.float64)
+    unit = np.exp(np.log(scale) * (-deg if op == "m2m" else deg + 1))
+    return src, xyz, pin, ref, unit
+
+
+@pytest.mark.parametrize("op", ["m2l", "m2m", "l2l"])
+def test_fp32_context_at_length_scales_its_storage_holds(native, oracle, op):
+    """The FP32 kernel (an SFMM_F32 context: FP32 expansions) runs every
+    translation at the length scale of its shift too; at scales whose
+    coefficients FP32 storage still holds (P=16: 1/8 ... 8) its error stays
+    the unit-scale one."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    P, n = 16, 48
+    S = P * (P + 1)
+    ctx = native.Context(P, "f32")
+    w = norm_weights_for(op, P)
+    for scale in (0.125, 0.5, 1.0, 2.0, 8.0):
+        src, xyz, pin, ref, unit = _scaled_batch(oracle, op, P, n, scale)
+        t_pin = torch.as_tensor(pin.astype(np.int32), device=dev)
+        out = torch.zeros(n, S, dtype=torch.float32, device=dev)
+        ctx.translate_device(op, 0, n, torch.as_tensor(src, dtype=torch.float32, device=dev), S, n, out, S, n,
+                             t_pin, t_pin, torch.as_tensor(xyz, device=dev), order_bound=P)
+        got = out.double().cpu().numpy()
+        assert np.isfinite(got).all(), (op, scale)
+        err = rel_err(got * unit, ref * unit, w)
+        assert err <= 2e-6, (op, scale, err)
+
+
 @pytest.mark.parametrize("op", ["m2l", "m2m", "l2l"])
 def test_every_mode_at_every_length_scale(ctx16, oracle, native, op):
     """The same tree shape at length scales 1e-9 ... 1e9: translations are
@@ -75,24 +122,9 @@ def test_every_mode_at_every_length_scale(ctx16, oracle, native, op):
     dev = torch.device("cuda", 0)
     P, n = 16, 48
     S = P * (P + 1)
-    deg = np.array([k for k in range(P) for _ in range(2 * k + 2)], dtype=np.float64)
     w = norm_weights_for(op, P)
     for scale in (1e-9, 1e-4, 1e-2, 1.0, 1e2, 1e4, 1e9):
-        rng = np.random.default_rng(5)
-        q = rng.choice([-1.0, 1.0], size=(n, 12))
-        d = rng.normal(size=(n, 12, 3))
-        d /= np.linalg.norm(d, axis=2, keepdims=True)
-        if op == "l2l":  # locals of far charges
-            src = oracle.p2m(P, q, (d * 0.4 + np.array([3.0, 0.5, -1.0])) * scale, np.zeros((n, 3)), singular=True)
-        else:
-            src = oracle.p2m(P, q, d * 0.4 * rng.random((n, 12, 1)) * scale, np.zeros((n, 3)))
-        u = rng.normal(size=(n, 3))
-        xyz = u / np.linalg.norm(u, axis=1, keepdims=True) * (3.0 if op == "m2l" else 0.5) * scale
-        pin = np.full(n, P, np.uint32)
-        ref = np.zeros((n, S))
-        oracle.naive(op, src, pin, ref, pin, xyz)
-        # unit-scale weights per coefficient: s^-n for multipoles, s^(n+1) for locals
-        unit = np.exp(np.log(scale) * (-deg if op == "m2m" else deg + 1))
+        src, xyz, pin, ref, unit = _scaled_batch(oracle, op, P, n, scale)
         t_pin = torch.as_tensor(pin.astype(np.int32), device=dev)
         t_src = torch.as_tensor(src, device=dev)
         t_xyz = torch.as_tensor(xyz, device=dev)
